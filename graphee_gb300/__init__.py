@@ -1,0 +1,387 @@
+"""graphee_gb300 — GraphMP's shard-wise gather-apply hot path on one GB300.
+
+Python side of the C ABI in ``include/gx.h`` (libgx.so, built in-tree by
+``graphee_gb300._build``).  It mirrors the reference's operator interface,
+``GraphPS<T>`` (GraphMP/system/GraphPS.h:22-63): ``init(path, V, P,
+max_iteration)`` then ``run()``, with the vertex program chosen by the app
+class (PagerankPS / SsspPS / CcPS, GraphMP/app/*.cpp) and ``init_vertex``
+overridable.  There is no CPU fallback: every compute call goes through
+libgx.so and fails loudly when it is missing or no GPU is visible.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "libgx.so"
+
+GX_OK, GX_ERR_INVALID, GX_ERR_IO, GX_ERR_FORMAT, GX_ERR_OOM, GX_ERR_CUDA, GX_ERR_TIMEOUT, \
+    GX_ERR_NODEVICE, GX_ERR_STATE = range(9)
+STATUS_NAMES = ["OK", "INVALID", "IO", "FORMAT", "OOM", "CUDA", "TIMEOUT", "NODEVICE", "STATE"]
+
+APP_PAGERANK_REF, APP_PAGERANK_STD, APP_SSSP, APP_CC, APP_INDEGREE = range(5)
+BUILD_DROP_SELF, BUILD_DEDUP, BUILD_SYMMETRIZE = 1, 2, 4
+GPS_INF = 10000          # GraphMP/system/Global.h:50
+INF_WEIGHTED = 0xFFFFFFFF
+
+
+class GxError(RuntimeError):
+    """A gx_status other than GX_OK, with gx_last_error()'s message."""
+
+    def __init__(self, status: int, where: str, msg: str):
+        self.status = status
+        name = STATUS_NAMES[status] if 0 <= status < len(STATUS_NAMES) else str(status)
+        super().__init__(f"{where}: GX_ERR_{name}: {msg}")
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("cache_budget_bytes", C.c_int64), ("stream_slots", C.c_int32),
+                ("selective_threshold", C.c_double), ("heavy_degree", C.c_int32), ("tile_edges", C.c_int32),
+                ("push_sparse", C.c_int32), ("use_graph", C.c_int32), ("wait_limit", C.c_uint32),
+                ("verbose", C.c_int32), ("profile", C.c_int32)]
+
+
+class RunParams(C.Structure):
+    _fields_ = [("app", C.c_int), ("max_iter", C.c_int32), ("damping", C.c_double), ("source", C.c_int32),
+                ("weighted", C.c_int32), ("tolerance", C.c_double), ("use_init", C.c_int32)]
+
+
+class RunStats(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("push_iterations", C.c_int32), ("changed_last", C.c_int64),
+                ("residual_l1_last", C.c_double), ("edges_scanned", C.c_int64), ("ms_total", C.c_double),
+                ("ms_copy", C.c_double), ("ms_compute", C.c_double), ("overlap", C.c_double),
+                ("h2d_bytes", C.c_int64), ("shards_resident", C.c_int32), ("shards_streamed", C.c_int32),
+                ("kernel_launches", C.c_int32), ("pull_launches", C.c_int32), ("ms_pull", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class IterStats(C.Structure):
+    _fields_ = [("changed", C.c_int64), ("active", C.c_int64), ("shards_active", C.c_int32),
+                ("mode", C.c_int32), ("residual_l1", C.c_double), ("dangling", C.c_double),
+                ("edges_scanned", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads libgx.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise RuntimeError(f"{LIB_PATH} is missing: run `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = C.CDLL(str(LIB_PATH))
+    P, I32, I64, U64, D = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_double
+    sig = {
+        "gx_config_default": (None, [P]),
+        "gx_run_params_default": (None, [P, C.c_int]),
+        "gx_last_error": (C.c_char_p, []),
+        "gx_create": (C.c_int, [P, P]),
+        "gx_destroy": (C.c_int, [P]),
+        "gx_load_shards": (C.c_int, [P, C.c_char_p, I32, I32]),
+        "gx_load_csc": (C.c_int, [P, I32, I32, P, P, P, P]),
+        "gx_set_weights": (C.c_int, [P, P]),
+        "gx_set_init": (C.c_int, [P, P]),
+        "gx_run": (C.c_int, [P, P, P]),
+        "gx_get_values": (C.c_int, [P, P]),
+        "gx_get_iter_stats": (C.c_int, [P, I32, P]),
+        "gx_rmat_edges": (C.c_int, [I32, I64, D, D, D, U64, I64, P, P]),
+        "gx_build_csc": (C.c_int, [I32, I64, P, P, I32, P, P, P]),
+        "gx_partition_bounds": (C.c_int, [I32, P, I32, P]),
+        "gx_out_degree": (C.c_int, [I32, P, P, P]),
+        "gx_write_shards": (C.c_int, [C.c_char_p, I32, I32, P, P, P, P]),
+        "gx_read_shards": (C.c_int, [C.c_char_p, I32, I32, P, P, P, P, P]),
+        "gx_edge_weights": (C.c_int, [U64, I32, P, P, P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(st: int, where: str) -> None:
+    if st != GX_OK:
+        raise GxError(st, where, lib().gx_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+# ---------------------------------------------------------------- graphs ----
+
+class Graph:
+    """A graph in the reference's shard layout, held as one global CSC:
+    bounds[P+1] destination ranges, off[V+1] in-edge offsets, col[E] source
+    ids (ascending per destination), outdeg[V]."""
+
+    def __init__(self, V, off, col, outdeg=None, P=1, bounds=None, weights=None):
+        self.V = int(V)
+        self.off = np.ascontiguousarray(off, dtype=np.int64)
+        self.col = np.ascontiguousarray(col, dtype=np.int32)
+        if outdeg is None:
+            outdeg = out_degree(self.V, self.off, self.col)
+        self.outdeg = np.ascontiguousarray(outdeg, dtype=np.int32)
+        self.P = int(P)
+        self.bounds = partition_bounds(self.V, self.off, self.P) if bounds is None else \
+            np.ascontiguousarray(bounds, dtype=np.int32)
+        self.weights = weights
+
+    @property
+    def E(self) -> int:
+        return int(self.off[-1])
+
+    def with_partitions(self, P: int) -> "Graph":
+        return Graph(self.V, self.off, self.col, self.outdeg, P, None, self.weights)
+
+
+def rmat_edges(scale: int, n: int, seed: int, a=0.57, b=0.19, c=0.19, first: int = 0):
+    src = np.empty(n, np.int32)
+    dst = np.empty(n, np.int32)
+    _check(lib().gx_rmat_edges(scale, n, a, b, c, seed & 0xFFFFFFFFFFFFFFFF, first, _ptr(src), _ptr(dst)),
+           "gx_rmat_edges")
+    return src, dst
+
+
+def build_csc(V: int, src, dst, flags=BUILD_DROP_SELF | BUILD_DEDUP):
+    src = np.ascontiguousarray(src, np.int32)
+    dst = np.ascontiguousarray(dst, np.int32)
+    n = len(src)
+    cap = 2 * n if flags & BUILD_SYMMETRIZE else n
+    off = np.empty(V + 1, np.int64)
+    col = np.empty(max(cap, 1), np.int32)
+    nout = C.c_int64(0)
+    _check(lib().gx_build_csc(V, n, _ptr(src), _ptr(dst), flags, _ptr(off), _ptr(col), C.byref(nout)),
+           "gx_build_csc")
+    return off, col[:nout.value].copy()
+
+
+def rmat_graph(scale: int, edge_factor: int, seed: int, P: int = 1, symmetric=False, a=0.57, b=0.19, c=0.19,
+               weight_seed: int | None = None) -> Graph:
+    """Seeded R-MAT graph, self-loops and duplicates removed (optionally
+    symmetrised), as a Graph with P edge-balanced shards."""
+    V = 1 << scale
+    src, dst = rmat_edges(scale, edge_factor * V, seed, a, b, c)
+    flags = BUILD_DROP_SELF | BUILD_DEDUP | (BUILD_SYMMETRIZE if symmetric else 0)
+    off, col = build_csc(V, src, dst, flags)
+    del src, dst
+    g = Graph(V, off, col, None, P)
+    if weight_seed is not None:
+        g.weights = edge_weights(weight_seed, g)
+    return g
+
+
+def partition_bounds(V: int, off: np.ndarray, P: int) -> np.ndarray:
+    bounds = np.empty(P + 1, np.int32)
+    _check(lib().gx_partition_bounds(V, _ptr(np.ascontiguousarray(off, np.int64)), P, _ptr(bounds)),
+           "gx_partition_bounds")
+    return bounds
+
+
+def out_degree(V: int, off: np.ndarray, col: np.ndarray) -> np.ndarray:
+    od = np.empty(V, np.int32)
+    _check(lib().gx_out_degree(V, _ptr(off), _ptr(col), _ptr(od)), "gx_out_degree")
+    return od
+
+
+def edge_weights(seed: int, g: Graph) -> np.ndarray:
+    w = np.empty(max(g.E, 1), np.uint32)
+    _check(lib().gx_edge_weights(seed & 0xFFFFFFFFFFFFFFFF, g.V, _ptr(g.off), _ptr(g.col), _ptr(w)),
+           "gx_edge_weights")
+    return w[:g.E]
+
+
+def write_shards(g: Graph, directory: str) -> str:
+    d = str(directory)
+    if not d.endswith("/"):
+        d += "/"
+    os.makedirs(d, exist_ok=True)
+    _check(lib().gx_write_shards(d.encode(), g.V, g.P, _ptr(g.bounds), _ptr(g.off), _ptr(g.col), _ptr(g.outdeg)),
+           "gx_write_shards")
+    return d
+
+
+def read_shards(directory: str, V: int, P: int) -> Graph:
+    d = str(directory)
+    if not d.endswith("/"):
+        d += "/"
+    E = C.c_int64(0)
+    _check(lib().gx_read_shards(d.encode(), V, P, None, None, None, None, C.byref(E)), "gx_read_shards")
+    bounds = np.empty(P + 1, np.int32)
+    off = np.empty(V + 1, np.int64)
+    col = np.empty(max(E.value, 1), np.int32)
+    od = np.empty(V, np.int32)
+    _check(lib().gx_read_shards(d.encode(), V, P, _ptr(bounds), _ptr(off), _ptr(col), _ptr(od), C.byref(E)),
+           "gx_read_shards")
+    return Graph(V, off, col[:E.value].copy(), od, P, bounds)
+
+
+# ---------------------------------------------------------------- engine ----
+
+def default_config(**kw) -> Config:
+    cfg = Config()
+    lib().gx_config_default(C.byref(cfg))
+    for k, v in kw.items():
+        setattr(cfg, k, v)
+    return cfg
+
+
+class Engine:
+    """One gx_engine (one GPU, one host thread)."""
+
+    def __init__(self, **config):
+        self.cfg = default_config(**config)
+        self._h = C.c_void_p()
+        _check(lib().gx_create(C.byref(self.cfg), C.byref(self._h)), "gx_create")
+        self.V = 0
+        self.app = None
+
+    def close(self):
+        if self._h:
+            lib().gx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def load(self, g: Graph) -> "Engine":
+        _check(lib().gx_load_csc(self._h, g.V, g.P, _ptr(g.bounds), _ptr(g.off), _ptr(g.col), _ptr(g.outdeg)),
+               "gx_load_csc")
+        self.V = g.V
+        if g.weights is not None:
+            self.set_weights(g.weights)
+        return self
+
+    def load_shards(self, directory: str, V: int, P: int) -> "Engine":
+        d = str(directory)
+        if not d.endswith("/"):
+            d += "/"
+        _check(lib().gx_load_shards(self._h, d.encode(), V, P), "gx_load_shards")
+        self.V = V
+        return self
+
+    def set_weights(self, w: np.ndarray) -> None:
+        w = np.ascontiguousarray(w, np.uint32)
+        _check(lib().gx_set_weights(self._h, _ptr(w)), "gx_set_weights")
+
+    def set_init(self, vals: np.ndarray) -> None:
+        vals = np.ascontiguousarray(vals)
+        if vals.itemsize != 4 or vals.size != self.V:
+            raise ValueError("initial values must be V 4-byte elements")
+        _check(lib().gx_set_init(self._h, _ptr(vals)), "gx_set_init")
+
+    def run(self, app: int, max_iter: int, damping=0.85, source=None, weighted=False, tolerance=0.0,
+            use_init=False) -> dict:
+        p = RunParams()
+        lib().gx_run_params_default(C.byref(p), app)
+        p.max_iter = max_iter
+        p.damping = damping
+        if source is not None:
+            p.source = source
+        p.weighted = int(weighted)
+        p.tolerance = tolerance
+        p.use_init = int(use_init)
+        st = RunStats()
+        _check(lib().gx_run(self._h, C.byref(p), C.byref(st)), "gx_run")
+        self.app = app
+        self._weighted = weighted
+        return st.as_dict()
+
+    def values(self) -> np.ndarray:
+        out = np.empty(self.V, np.uint32)
+        _check(lib().gx_get_values(self._h, _ptr(out)), "gx_get_values")
+        if self.app in (APP_PAGERANK_REF, APP_PAGERANK_STD):
+            return out.view(np.float32)
+        if self.app == APP_SSSP and self._weighted:
+            return out
+        return out.view(np.int32)
+
+    def iter_stats(self, step: int) -> dict:
+        s = IterStats()
+        _check(lib().gx_get_iter_stats(self._h, step, C.byref(s)), "gx_get_iter_stats")
+        return s.as_dict()
+
+
+# ------------------------------------------- the reference's app interface ----
+
+class GraphPS:
+    """Mirror of GraphPS<T> (GraphMP/system/GraphPS.h:22-63).
+
+    ``init(data_path, vertex_num, partition_num, max_iteration=10)`` loads
+    the shard directory (GraphPS.h:77); ``run()`` runs the superstep loop
+    (GraphPS.h:171) on the GPU; after it ``vertex_msg`` holds _VertexMsg.
+    Subclasses choose the vertex program (``app``) and may override
+    ``init_vertex()`` to return initial values (GraphPS.h:60)."""
+
+    app = APP_PAGERANK_REF
+
+    def __init__(self, **config):
+        self._engine = Engine(**config)
+        self._DataPath = ""
+        self._VertexNum = 0
+        self._PartitionNum = 0
+        self._MaxIteration = 0
+        self.vertex_msg = None
+        self.stats = None
+
+    def init(self, data_path: str, vertex_num: int, partition_num: int, max_iteration: int = 10):
+        self._DataPath = data_path
+        self._VertexNum = vertex_num
+        self._PartitionNum = partition_num
+        self._MaxIteration = max_iteration
+        self._engine.load_shards(data_path, vertex_num, partition_num)
+
+    def init_vertex(self):
+        """Return initial vertex values, or None for the app's own init."""
+        return None
+
+    def run_params(self) -> dict:
+        return {}
+
+    def run(self):
+        init = self.init_vertex()
+        if init is not None:
+            self._engine.set_init(init)
+        self.stats = self._engine.run(self.app, self._MaxIteration, use_init=init is not None, **self.run_params())
+        self.vertex_msg = self._engine.values()
+        return self.stats
+
+
+class PagerankPS(GraphPS):
+    """GraphMP/app/pagerank.cpp: PagerankPS<float>."""
+    app = APP_PAGERANK_REF
+
+
+class SsspPS(GraphPS):
+    """GraphMP/app/sssp.cpp: unit-weight SSSP from vertex 1 (``source`` moves it)."""
+    app = APP_SSSP
+    source = 1
+
+    def run_params(self):
+        return {"source": self.source}
+
+
+class CcPS(GraphPS):
+    """GraphMP/app/cc.cpp: min-label connected components."""
+    app = APP_CC

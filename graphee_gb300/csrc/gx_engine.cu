@@ -1,0 +1,980 @@
+// The engine behind the C ABI: GraphPS<T> (GraphMP/system/GraphPS.h:22-387)
+// re-designed for one GB300.
+//
+// HBM layout (all-resident case):
+//   off     int64[V+1]   global CSC offsets (the shards' indptr, rebased)
+//   col     int32[E+4]   source ids, shards laid end to end (the shards' indices)
+//   w       uint32[E+4]  SSSP weights aligned with col (optional)
+//   outdeg  int32[V]     vertexout.npy
+//   val     T[2][V]      Msg / MsgNew as a double buffer (swap instead of copy)
+//   con     f32[2][V]    PageRank contributions Msg[u]/outdeg[u]
+//   units   int2[U]      warp work units, unit_shard int32[U]
+//   bm      u32[V/32+2]  next-frontier bitmap; frontier int2[V]
+//   sig     u64[V]       per-vertex shard-group mask (selective scheduling)
+//   ooff/ocol/ow         out-edge CSR for sparse push steps (SSSP/CC)
+// With a shard-cache budget, only the shards that fit stay in HBM; the others
+// are kept in pinned host memory and streamed per step through a ring of
+// device slots on a copy stream (the GPU form of load_edge, Global.h:129-255).
+#include <cuda_runtime.h>
+#include <omp.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "gx_internal.h"
+#include "gx_kernels.cuh"
+
+using namespace gx;
+
+#define GX_CUDA(call)                                                                                   \
+  do {                                                                                                  \
+    cudaError_t err_ = (call);                                                                          \
+    if (err_ != cudaSuccess)                                                                            \
+      return fail(err_ == cudaErrorMemoryAllocation ? GX_ERR_OOM : GX_ERR_CUDA, "%s:%d %s: %s", __FILE__, \
+                  __LINE__, #call, cudaGetErrorString(err_));                                          \
+  } while (0)
+
+#define GX_TRY(call)                 \
+  do {                               \
+    gx_status st_ = (call);          \
+    if (st_ != GX_OK) return st_;    \
+  } while (0)
+
+namespace {
+
+template <class T>
+gx_status dev_alloc(T** p, size_t n) {
+  if (*p) {
+    cudaFree(*p);
+    *p = nullptr;
+  }
+  if (n == 0) n = 1;
+  cudaError_t err = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+  if (err != cudaSuccess) {
+    *p = nullptr;
+    cudaGetLastError();
+    return fail(GX_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(err));
+  }
+  return GX_OK;
+}
+
+template <class T>
+void dev_free(T** p) {
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+}
+
+int app_kind(const gx_run_params& p) {
+  switch (p.app) {
+    case GX_APP_PAGERANK_REF: return K_PR_REF;
+    case GX_APP_PAGERANK_STD: return K_PR_STD;
+    case GX_APP_SSSP: return p.weighted ? K_SSSP_W : K_SSSP_UNIT;
+    case GX_APP_CC: return K_CC;
+    case GX_APP_INDEGREE: return K_INDEG;
+  }
+  return -1;
+}
+
+}  // namespace
+
+struct gx_engine {
+  gx_config cfg{};
+  int dev = 0;
+  int n_sm = 0;
+  cudaStream_t s_comp = nullptr, s_copy = nullptr;
+  bool loaded = false;
+
+  // graph (host side)
+  int32_t V = 0, P = 0;
+  int64_t E = 0;
+  std::vector<int32_t> bounds;
+  std::vector<int64_t> off;
+  std::vector<int32_t> outdeg;
+  std::vector<int2> units;
+  std::vector<int32_t> unit_shard;
+  std::vector<int32_t> unit_begin;  // P+1
+  std::vector<int4> heavy;
+  int64_t n_partials = 0;
+
+  // shard cache
+  std::vector<char> resident;
+  std::vector<int64_t> dev_base;    // element offset of a resident shard's slice in d_col
+  int32_t n_resident = 0;
+  bool all_resident = true;
+  int32_t* h_col = nullptr;         // pinned full copy when some shards stream
+  uint32_t* h_w = nullptr;
+  int64_t slot_elems = 0;
+  std::vector<int32_t*> slot_col;
+  std::vector<uint32_t*> slot_w;
+  std::vector<cudaEvent_t> slot_free, slot_ready;
+
+  // device
+  int64_t* d_off = nullptr;
+  int32_t* d_col = nullptr;
+  uint32_t* d_w = nullptr;
+  bool has_weights = false;
+  std::vector<uint32_t> w_host;     // kept until the shard plan is fixed
+  int32_t* d_outdeg = nullptr;
+  void* d_val[2] = {nullptr, nullptr};
+  float* d_con[2] = {nullptr, nullptr};
+  int2* d_units = nullptr;
+  int32_t* d_unit_shard = nullptr;
+  int4* d_heavy = nullptr;
+  void* d_partial = nullptr;
+  unsigned int* d_hticket = nullptr;
+  uint32_t* d_bm = nullptr;
+  int32_t n_words = 0;
+  unsigned long long* d_sig = nullptr;
+  int2* d_frontier = nullptr;
+  int64_t* d_ooff = nullptr;
+  int32_t* d_ocol = nullptr;
+  uint32_t* d_ow = nullptr;
+  bool out_built = false, out_weighted = false;
+  Ctl* d_ctl = nullptr;
+  Ctl* h_ctl = nullptr;
+  StepStats* d_stats = nullptr;
+  int32_t stats_cap = 0;
+  unsigned int* d_work = nullptr;
+  int32_t n_work = 0;
+  int32_t shard_group = 1;
+
+  std::vector<uint32_t> init_vals;
+  bool has_init = false;
+
+  // last run
+  gx_app last_app = GX_APP_PAGERANK_REF;
+  int32_t last_steps = 0;
+  std::vector<StepStats> last_stats;
+  gx_run_stats last_run{};
+
+  ~gx_engine() { release(); }
+
+  void release_graph() {
+    dev_free(&d_off);
+    dev_free(&d_col);
+    dev_free(&d_w);
+    dev_free(&d_outdeg);
+    for (int i = 0; i < 2; ++i) {
+      dev_free(&d_val[i]);
+      dev_free(&d_con[i]);
+    }
+    dev_free(&d_units);
+    dev_free(&d_unit_shard);
+    dev_free(&d_heavy);
+    dev_free(&d_partial);
+    dev_free(&d_hticket);
+    dev_free(&d_bm);
+    dev_free(&d_sig);
+    dev_free(&d_frontier);
+    dev_free(&d_ooff);
+    dev_free(&d_ocol);
+    dev_free(&d_ow);
+    dev_free(&d_stats);
+    dev_free(&d_work);
+    for (auto p : slot_col) cudaFree(p);
+    for (auto p : slot_w) cudaFree(p);
+    slot_col.clear();
+    slot_w.clear();
+    for (auto ev : slot_free) cudaEventDestroy(ev);
+    for (auto ev : slot_ready) cudaEventDestroy(ev);
+    slot_free.clear();
+    slot_ready.clear();
+    if (h_col) cudaFreeHost(h_col);
+    if (h_w) cudaFreeHost(h_w);
+    h_col = nullptr;
+    h_w = nullptr;
+    out_built = false;
+    has_weights = false;
+    loaded = false;
+    stats_cap = 0;
+  }
+
+  void release() {
+    cudaSetDevice(dev);
+    release_graph();
+    dev_free(&d_ctl);
+    if (h_ctl) cudaFreeHost(h_ctl);
+    h_ctl = nullptr;
+    if (s_comp) cudaStreamDestroy(s_comp);
+    if (s_copy) cudaStreamDestroy(s_copy);
+    s_comp = s_copy = nullptr;
+  }
+};
+
+namespace {
+
+// Work units of one shard: heavy-vertex chunks first, then tiles of up to 32
+// consecutive light vertices with at most tile_edges edges.
+void build_units(gx_engine* e) {
+  const int32_t P = e->P;
+  const int64_t* off = e->off.data();
+  const int32_t heavy_deg = std::max(e->cfg.heavy_degree, 32);
+  const int64_t cap = std::max<int64_t>(e->cfg.tile_edges, 32);
+  std::vector<std::vector<int2>> su(P);
+  std::vector<std::vector<int32_t>> sh(P);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int32_t p = 0; p < P; ++p) {
+    std::vector<int2>& U = su[p];
+    const int32_t s = e->bounds[p], t = e->bounds[p + 1];
+    int32_t vb = s, cnt = 0;
+    int64_t edges = 0;
+    auto close = [&](int32_t ve) {
+      if (cnt > 0) U.push_back(make_int2(vb, ve));
+      cnt = 0;
+      edges = 0;
+    };
+    for (int32_t v = s; v < t; ++v) {
+      const int64_t d = off[v + 1] - off[v];
+      if (d > heavy_deg) {
+        close(v);
+        sh[p].push_back(v);
+        vb = v + 1;
+        continue;
+      }
+      if (cnt == 32 || (cnt > 0 && edges + d > cap)) {
+        close(v);
+        vb = v;
+      }
+      if (cnt == 0) vb = v;
+      ++cnt;
+      edges += d;
+    }
+    close(t);
+  }
+  e->units.clear();
+  e->unit_shard.clear();
+  e->heavy.clear();
+  e->unit_begin.assign(P + 1, 0);
+  int64_t partials = 0;
+  for (int32_t p = 0; p < P; ++p) {
+    e->unit_begin[p] = static_cast<int32_t>(e->units.size());
+    // Longest heavy vertices first within the shard.
+    std::vector<int32_t>& hv = sh[p];
+    std::sort(hv.begin(), hv.end(), [&](int32_t a, int32_t b) {
+      const int64_t da = off[a + 1] - off[a], db = off[b + 1] - off[b];
+      return da > db || (da == db && a < b);
+    });
+    for (int32_t v : hv) {
+      const int64_t d = off[v + 1] - off[v];
+      const int32_t nch = static_cast<int32_t>((d + kHeavyChunk - 1) / kHeavyChunk);
+      const int32_t h = static_cast<int32_t>(e->heavy.size());
+      e->heavy.push_back(make_int4(v, nch, static_cast<int32_t>(partials), p));
+      for (int32_t c = 0; c < nch; ++c) {
+        e->units.push_back(make_int2(-(h + 1), c));
+        e->unit_shard.push_back(p);
+      }
+      partials += nch;
+    }
+    for (const int2& u : su[p]) {
+      e->units.push_back(u);
+      e->unit_shard.push_back(p);
+    }
+  }
+  e->unit_begin[P] = static_cast<int32_t>(e->units.size());
+  e->n_partials = partials;
+}
+
+gx_status alloc_ctl(gx_engine* e) {
+  if (!e->d_ctl) GX_TRY(dev_alloc(&e->d_ctl, 1));
+  if (!e->h_ctl) GX_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->h_ctl), sizeof(Ctl), cudaHostAllocDefault));
+  return GX_OK;
+}
+
+// Decides which shards stay in HBM under the budget (in shard order, like the
+// reference's insert-until-full edge cache, Global.h:170-244), uploads them,
+// and sets up the streaming ring for the rest.
+gx_status plan_shards(gx_engine* e) {
+  const int32_t P = e->P;
+  const int64_t per_edge = e->has_weights ? 8 : 4;
+  const int64_t budget = e->cfg.cache_budget_bytes;
+  e->resident.assign(P, 0);
+  e->dev_base.assign(P, 0);
+  int64_t used = 0, max_stream = 0;
+  e->n_resident = 0;
+  std::vector<int64_t> lo(P), hi(P);
+  for (int32_t p = 0; p < P; ++p) {
+    lo[p] = e->off[e->bounds[p]] & ~3ll;
+    hi[p] = (e->off[e->bounds[p + 1]] + 3) & ~3ll;
+    const int64_t bytes = (hi[p] - lo[p] + 4) * per_edge;
+    if (budget < 0 || used + bytes <= budget) {
+      e->resident[p] = 1;
+      used += hi[p] - lo[p] + 4;
+      ++e->n_resident;
+    } else {
+      max_stream = std::max(max_stream, hi[p] - lo[p] + 4);
+    }
+  }
+  e->all_resident = e->n_resident == P;
+  dev_free(&e->d_col);
+  dev_free(&e->d_w);
+  if (e->all_resident) {
+    GX_TRY(dev_alloc(&e->d_col, static_cast<size_t>(e->E) + 8));
+    GX_CUDA(cudaMemset(e->d_col, 0, (e->E + 8) * sizeof(int32_t)));
+    const int32_t* src = e->h_col;
+    GX_CUDA(cudaMemcpy(e->d_col, src, e->E * sizeof(int32_t), cudaMemcpyHostToDevice));
+    if (e->has_weights) {
+      GX_TRY(dev_alloc(&e->d_w, static_cast<size_t>(e->E) + 8));
+      GX_CUDA(cudaMemset(e->d_w, 0, (e->E + 8) * sizeof(uint32_t)));
+      GX_CUDA(cudaMemcpy(e->d_w, e->h_w, e->E * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    }
+    for (int32_t p = 0; p < P; ++p) e->dev_base[p] = 0;
+  } else {
+    GX_TRY(dev_alloc(&e->d_col, static_cast<size_t>(used) + 8));
+    if (e->has_weights) GX_TRY(dev_alloc(&e->d_w, static_cast<size_t>(used) + 8));
+    int64_t pos = 0;
+    for (int32_t p = 0; p < P; ++p) {
+      if (!e->resident[p]) continue;
+      const int64_t n = std::min(hi[p], e->E + 4) - lo[p];
+      GX_CUDA(cudaMemcpy(e->d_col + pos, e->h_col + lo[p], n * sizeof(int32_t), cudaMemcpyHostToDevice));
+      if (e->has_weights)
+        GX_CUDA(cudaMemcpy(e->d_w + pos, e->h_w + lo[p], n * sizeof(uint32_t), cudaMemcpyHostToDevice));
+      e->dev_base[p] = pos - lo[p];  // d_col + dev_base[p] is indexed by global edge id
+      pos += hi[p] - lo[p] + 4;
+    }
+    const int slots = std::max(2, e->cfg.stream_slots);
+    e->slot_elems = max_stream + 8;
+    for (auto ptr : e->slot_col) cudaFree(ptr);
+    for (auto ptr : e->slot_w) cudaFree(ptr);
+    e->slot_col.assign(slots, nullptr);
+    e->slot_w.assign(slots, nullptr);
+    for (int i = 0; i < slots; ++i) {
+      GX_TRY(dev_alloc(&e->slot_col[i], e->slot_elems));
+      if (e->has_weights) GX_TRY(dev_alloc(&e->slot_w[i], e->slot_elems));
+    }
+    if (e->slot_free.empty()) {
+      e->slot_free.resize(slots);
+      e->slot_ready.resize(slots);
+      for (int i = 0; i < slots; ++i) {
+        GX_CUDA(cudaEventCreateWithFlags(&e->slot_free[i], cudaEventDisableTiming));
+        GX_CUDA(cudaEventCreateWithFlags(&e->slot_ready[i], cudaEventDisableTiming));
+      }
+    }
+  }
+  e->out_built = false;
+  return GX_OK;
+}
+
+// Per-vertex shard-group masks, built shard by shard (streamed shards go
+// through slot 0).
+gx_status build_signatures(gx_engine* e) {
+  const int32_t P = e->P;
+  e->shard_group = (P + 63) / 64;
+  GX_TRY(dev_alloc(&e->d_sig, static_cast<size_t>(e->V)));
+  GX_CUDA(cudaMemsetAsync(e->d_sig, 0, sizeof(unsigned long long) * e->V, e->s_comp));
+  for (int32_t p = 0; p < P; ++p) {
+    const int64_t e0 = e->off[e->bounds[p]], e1 = e->off[e->bounds[p + 1]];
+    if (e1 == e0) continue;
+    const int32_t* col = nullptr;
+    if (e->all_resident) {
+      col = e->d_col;
+    } else if (e->resident[p]) {
+      col = e->d_col + e->dev_base[p];
+    } else {
+      const int64_t lo = e0 & ~3ll;
+      GX_CUDA(cudaMemcpyAsync(e->slot_col[0], e->h_col + lo, (e1 - lo) * sizeof(int32_t), cudaMemcpyHostToDevice,
+                              e->s_comp));
+      col = e->slot_col[0] - lo;
+    }
+    const unsigned long long bit = 1ull << (p / e->shard_group);
+    const int64_t n = e1 - e0;
+    const int grid = static_cast<int>(std::min<int64_t>((n + 255) / 256, static_cast<int64_t>(e->n_sm) * 8));
+    signature_kernel<<<grid, 256, 0, e->s_comp>>>(e->d_sig, col, e0, e1, bit);
+    GX_CUDA(cudaGetLastError());
+  }
+  GX_CUDA(cudaStreamSynchronize(e->s_comp));
+  return GX_OK;
+}
+
+// Out-edge CSR for push steps (all-resident graphs only).
+gx_status build_out_edges(gx_engine* e, bool weighted) {
+  if (e->out_built && (!weighted || e->out_weighted)) return GX_OK;
+  const int32_t V = e->V;
+  std::vector<int64_t> ooff(static_cast<size_t>(V) + 1, 0);
+  for (int32_t v = 0; v < V; ++v) ooff[v + 1] = ooff[v] + e->outdeg[v];
+  if (ooff[V] != e->E)
+    return fail(GX_ERR_FORMAT, "vertexout.npy sums to %lld out-edges but the shards hold %lld edges",
+                static_cast<long long>(ooff[V]), static_cast<long long>(e->E));
+  GX_TRY(dev_alloc(&e->d_ooff, static_cast<size_t>(V) + 1));
+  GX_TRY(dev_alloc(&e->d_ocol, static_cast<size_t>(e->E) + 8));
+  if (weighted) GX_TRY(dev_alloc(&e->d_ow, static_cast<size_t>(e->E) + 8));
+  unsigned long long* cursor = nullptr;
+  GX_TRY(dev_alloc(&cursor, static_cast<size_t>(V) + 1));
+  GX_CUDA(cudaMemcpy(e->d_ooff, ooff.data(), ooff.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+  GX_CUDA(cudaMemcpy(cursor, ooff.data(), ooff.size() * sizeof(int64_t), cudaMemcpyHostToDevice));
+  transpose_kernel<<<e->n_sm * 8, 256, 0, e->s_comp>>>(e->d_off, e->d_col, weighted ? e->d_w : nullptr, V, cursor,
+                                                        e->d_ocol, weighted ? e->d_ow : nullptr);
+  cudaError_t err = cudaGetLastError();
+  if (err == cudaSuccess) err = cudaStreamSynchronize(e->s_comp);
+  cudaFree(cursor);
+  if (err != cudaSuccess) return fail(GX_ERR_CUDA, "transpose: %s", cudaGetErrorString(err));
+  e->out_built = true;
+  e->out_weighted = weighted;
+  return GX_OK;
+}
+
+template <int APP>
+int occupancy_grid(gx_engine* e, const void* fn) {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kThreads, 0);
+  return std::max(1, per_sm) * e->n_sm;
+}
+
+template <int APP>
+gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
+  typedef typename AppTraits<APP>::T T;
+  const int32_t V = e->V;
+  const bool weighted = APP == K_SSSP_W;
+  const bool min_app = APP == K_SSSP_UNIT || APP == K_SSSP_W || APP == K_CC;
+  const bool push_ok = min_app && e->cfg.push_sparse && e->all_resident;
+  if (push_ok) GX_TRY(build_out_edges(e, weighted));
+  if (e->stats_cap < prm.max_iter) {
+    GX_TRY(dev_alloc(&e->d_stats, static_cast<size_t>(std::max(prm.max_iter, 1))));
+    e->stats_cap = prm.max_iter;
+  }
+
+  // Control block.
+  Ctl c{};
+  c.max_iter = prm.max_iter;
+  c.n_vertices = V;
+  c.n_shards = e->P;
+  c.shard_group = e->shard_group;
+  c.push_ok = push_ok;
+  c.damping = prm.damping;
+  c.inv_n = 1.0 / V;
+  c.fx_scale = static_cast<double>(V) * 1073741824.0;  // 2^30 per 1/N of rank
+  c.tolerance = prm.tolerance;
+  c.sel_threshold = e->cfg.selective_threshold;
+  c.step = 0;
+  c.cur = 0;
+  c.mode = MODE_DENSE;
+  c.done = prm.max_iter <= 0;
+  c.shard_mask = ~0ull;
+  // Initial values: init_vertex of the app, or the caller's values.
+  int use_init = 0;
+  if (prm.use_init) {
+    if (!e->has_init) return fail(GX_ERR_STATE, "gx_run: use_init set but gx_set_init was not called");
+    GX_CUDA(cudaMemcpy(e->d_val[0], e->init_vals.data(), sizeof(T) * V, cudaMemcpyHostToDevice));
+    use_init = 1;
+  }
+  if (APP == K_PR_STD) {
+    // D of the initial vector, in the same fixed point the device uses.
+    double D = 0;
+    int64_t n_dangling = 0;
+    for (int32_t v = 0; v < V; ++v) {
+      if (e->outdeg[v] != 0) continue;
+      ++n_dangling;
+      if (use_init) {
+        float x;
+        memcpy(&x, &e->init_vals[v], sizeof(float));
+        D += x;
+      }
+    }
+    if (!use_init) D = static_cast<double>(n_dangling) * static_cast<double>(static_cast<float>(1.0 / V));
+    c.base = (1.0 - prm.damping) * c.inv_n + prm.damping * D * c.inv_n;
+  }
+  GX_CUDA(cudaMemcpyAsync(e->d_ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, e->s_comp));
+  init_kernel<APP><<<e->n_sm * 4, 256, 0, e->s_comp>>>(e->d_ctl, e->d_val[0], e->d_con[0], e->d_outdeg, V,
+                                                       prm.source, use_init);
+  GX_CUDA(cudaGetLastError());
+  GX_CUDA(cudaMemsetAsync(e->d_bm, 0, sizeof(uint32_t) * e->n_words, e->s_comp));
+  GX_CUDA(cudaMemsetAsync(e->d_work, 0, sizeof(unsigned int) * e->n_work, e->s_comp));
+  GX_CUDA(cudaMemsetAsync(e->d_hticket, 0, sizeof(unsigned int) * std::max<size_t>(e->heavy.size(), 1), e->s_comp));
+
+  PullArgs pa{};
+  pa.ctl = e->d_ctl;
+  pa.off = e->d_off;
+  pa.col = e->d_col;
+  pa.w = e->d_w;
+  pa.outdeg = e->d_outdeg;
+  pa.val[0] = e->d_val[0];
+  pa.val[1] = e->d_val[1];
+  pa.con[0] = e->d_con[0];
+  pa.con[1] = e->d_con[1];
+  pa.units = e->d_units;
+  pa.unit_shard = e->d_unit_shard;
+  pa.u_begin = 0;
+  pa.u_end = static_cast<int32_t>(e->units.size());
+  pa.heavy = e->d_heavy;
+  pa.partial = e->d_partial;
+  pa.hticket = e->d_hticket;
+  pa.bm = e->d_bm;
+  PushArgs qa{};
+  qa.ctl = e->d_ctl;
+  qa.ooff = e->d_ooff;
+  qa.ocol = e->d_ocol;
+  qa.ow = e->d_ow;
+  qa.val[0] = e->d_val[0];
+  qa.val[1] = e->d_val[1];
+  qa.frontier = e->d_frontier;
+  qa.ctr = e->d_work;
+  qa.bm = e->d_bm;
+  FinArgs fa{};
+  fa.ctl = e->d_ctl;
+  fa.stats = e->d_stats;
+  fa.bm = e->d_bm;
+  fa.n_words = e->n_words;
+  fa.sig = e->d_sig;
+  fa.val[0] = e->d_val[0];
+  fa.val[1] = e->d_val[1];
+  fa.frontier = e->d_frontier;
+  fa.work_ctr = e->d_work;
+  fa.n_work_ctr = e->n_work;
+
+  const int grid_pull = occupancy_grid<APP>(e, reinterpret_cast<const void*>(pull_kernel<APP>));
+  const int grid_push = occupancy_grid<APP>(e, reinterpret_cast<const void*>(push_kernel<APP>));
+  const int grid_fin = std::max(1, std::min(e->n_sm * 4, (e->n_words + kThreads - 1) / kThreads));
+
+  cudaEvent_t ev0, ev1;
+  GX_CUDA(cudaEventCreate(&ev0));
+  GX_CUDA(cudaEventCreate(&ev1));
+  std::unique_ptr<cudaEvent_t, void (*)(cudaEvent_t*)> g0(&ev0, [](cudaEvent_t* x) { cudaEventDestroy(*x); });
+  std::unique_ptr<cudaEvent_t, void (*)(cudaEvent_t*)> g1(&ev1, [](cudaEvent_t* x) { cudaEventDestroy(*x); });
+  int64_t h2d_bytes = 0;
+  int32_t streamed = 0;
+  int32_t launches = 1;  // init_kernel
+  int32_t pull_launches = 0;
+  double ms_pull = 0;
+  double copy_ms = 0, comp_ms = 0;
+
+  GX_CUDA(cudaEventRecord(ev0, e->s_comp));
+  if (e->all_resident) {
+    // Replay K supersteps per CUDA graph launch; the control block makes
+    // steps after termination no-ops.
+    const int K = std::max(1, std::min(prm.max_iter, 8));
+    const bool prof = e->cfg.profile != 0;
+    std::vector<cudaEvent_t> pev(prof ? 2 * K : 0);
+    for (auto& ev : pev) GX_CUDA(cudaEventCreate(&ev));
+    std::unique_ptr<std::vector<cudaEvent_t>, void (*)(std::vector<cudaEvent_t>*)> pev_guard(
+        &pev, [](std::vector<cudaEvent_t>* v) {
+          for (auto ev : *v) cudaEventDestroy(ev);
+        });
+    auto enqueue = [&](int i) -> gx_status {
+      if (prof) GX_CUDA(cudaEventRecord(pev[2 * i], e->s_comp));
+      pull_kernel<APP><<<grid_pull, kThreads, 0, e->s_comp>>>(pa);
+      if (prof) GX_CUDA(cudaEventRecord(pev[2 * i + 1], e->s_comp));
+      if (push_ok) push_kernel<APP><<<grid_push, kThreads, 0, e->s_comp>>>(qa);
+      finalize_kernel<APP><<<grid_fin, kThreads, 0, e->s_comp>>>(fa);
+      GX_CUDA(cudaGetLastError());
+      launches += push_ok ? 3 : 2;
+      return GX_OK;
+    };
+    cudaGraphExec_t exec = nullptr;
+    // Profiling times each pull launch with its own events, so it launches
+    // directly instead of replaying a graph.
+    if (e->cfg.use_graph && !prof) {
+      cudaGraph_t graph;
+      GX_CUDA(cudaStreamBeginCapture(e->s_comp, cudaStreamCaptureModeThreadLocal));
+      for (int i = 0; i < K; ++i) {
+        gx_status st = enqueue(i);
+        if (st != GX_OK) {
+          cudaStreamEndCapture(e->s_comp, &graph);
+          return st;
+        }
+      }
+      GX_CUDA(cudaStreamEndCapture(e->s_comp, &graph));
+      cudaError_t err = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      if (err != cudaSuccess) return fail(GX_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(err));
+      launches = 0;
+    }
+    const int per_step = push_ok ? 3 : 2;
+    int steps_before = 0;
+    for (int launched = 0; launched < prm.max_iter; launched += K) {
+      if (exec) {
+        GX_CUDA(cudaGraphLaunch(exec, e->s_comp));
+        launches += K * per_step;
+      } else {
+        for (int i = 0; i < K; ++i) GX_TRY(enqueue(i));
+      }
+      GX_CUDA(cudaMemcpyAsync(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->s_comp));
+      cudaError_t err = cudaStreamSynchronize(e->s_comp);
+      if (err != cudaSuccess) {
+        if (exec) cudaGraphExecDestroy(exec);
+        return fail(GX_ERR_CUDA, "superstep loop: %s", cudaGetErrorString(err));
+      }
+      const int ran = std::min(K, e->h_ctl->step - steps_before);
+      for (int i = 0; i < ran && prof; ++i) {
+        float t = 0;
+        GX_CUDA(cudaEventElapsedTime(&t, pev[2 * i], pev[2 * i + 1]));
+        ms_pull += t;
+      }
+      pull_launches += ran;
+      steps_before = e->h_ctl->step;
+      if (e->h_ctl->done) break;
+    }
+    if (exec) cudaGraphExecDestroy(exec);
+  } else {
+    // Host-driven steps: shard launches in order, streamed shards through
+    // the slot ring on the copy stream, overlapped with compute.
+    const int slots = static_cast<int>(e->slot_col.size());
+    cudaEvent_t c0, c1, k0, k1;
+    GX_CUDA(cudaEventCreate(&c0));
+    GX_CUDA(cudaEventCreate(&c1));
+    GX_CUDA(cudaEventCreate(&k0));
+    GX_CUDA(cudaEventCreate(&k1));
+    int slot = 0;
+    for (int step = 0; step < prm.max_iter; ++step) {
+      GX_CUDA(cudaMemcpyAsync(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->s_comp));
+      GX_CUDA(cudaStreamSynchronize(e->s_comp));
+      const Ctl& hc = *e->h_ctl;
+      if (hc.done) break;
+      const bool sel = hc.mode == MODE_SELECTIVE;
+      GX_CUDA(cudaEventRecord(c0, e->s_copy));
+      GX_CUDA(cudaEventRecord(k0, e->s_comp));
+      for (int32_t p = 0; p < e->P; ++p) {
+        PullArgs sp = pa;
+        sp.u_begin = e->unit_begin[p];
+        sp.u_end = e->unit_begin[p + 1];
+        if (sp.u_end == sp.u_begin) continue;
+        const bool active = !sel || ((hc.shard_mask >> (p / e->shard_group)) & 1ull);
+        if (e->resident[p] || !active) {
+          sp.col = e->d_col + e->dev_base[p];
+          if (e->d_w) sp.w = e->d_w + e->dev_base[p];
+        } else {
+          const int64_t lo = e->off[e->bounds[p]] & ~3ll;
+          const int64_t n = std::min<int64_t>((e->off[e->bounds[p + 1]] + 3) & ~3ll, e->E + 4) - lo;
+          GX_CUDA(cudaStreamWaitEvent(e->s_copy, e->slot_free[slot], 0));
+          GX_CUDA(cudaMemcpyAsync(e->slot_col[slot], e->h_col + lo, n * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                  e->s_copy));
+          h2d_bytes += n * sizeof(int32_t);
+          if (weighted) {
+            GX_CUDA(cudaMemcpyAsync(e->slot_w[slot], e->h_w + lo, n * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                    e->s_copy));
+            h2d_bytes += n * sizeof(uint32_t);
+          }
+          GX_CUDA(cudaEventRecord(e->slot_ready[slot], e->s_copy));
+          GX_CUDA(cudaStreamWaitEvent(e->s_comp, e->slot_ready[slot], 0));
+          sp.col = e->slot_col[slot] - lo;
+          if (weighted) sp.w = e->slot_w[slot] - lo;
+          ++streamed;
+        }
+        const int units = sp.u_end - sp.u_begin;
+        const int grid = std::max(1, std::min(grid_pull, (units + kWarps - 1) / kWarps));
+        pull_kernel<APP><<<grid, kThreads, 0, e->s_comp>>>(sp);
+        GX_CUDA(cudaGetLastError());
+        ++launches;
+        ++pull_launches;
+        if (!e->resident[p] && active) {
+          GX_CUDA(cudaEventRecord(e->slot_free[slot], e->s_comp));
+          slot = (slot + 1) % slots;
+        }
+      }
+      GX_CUDA(cudaEventRecord(c1, e->s_copy));
+      GX_CUDA(cudaEventRecord(k1, e->s_comp));
+      finalize_kernel<APP><<<grid_fin, kThreads, 0, e->s_comp>>>(fa);
+      GX_CUDA(cudaGetLastError());
+      ++launches;
+      GX_CUDA(cudaStreamSynchronize(e->s_copy));
+      GX_CUDA(cudaStreamSynchronize(e->s_comp));
+      float ms_c = 0, ms_k = 0;
+      cudaEventElapsedTime(&ms_c, c0, c1);
+      cudaEventElapsedTime(&ms_k, k0, k1);
+      copy_ms += ms_c;
+      comp_ms += ms_k;
+    }
+    cudaEventDestroy(c0);
+    cudaEventDestroy(c1);
+    cudaEventDestroy(k0);
+    cudaEventDestroy(k1);
+  }
+  GX_CUDA(cudaEventRecord(ev1, e->s_comp));
+  GX_CUDA(cudaEventSynchronize(ev1));
+  GX_CUDA(cudaMemcpy(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  float ms = 0;
+  GX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
+
+  const int32_t steps = e->h_ctl->step;
+  e->last_steps = steps;
+  e->last_stats.assign(std::max(steps, 0), StepStats{});
+  if (steps > 0)
+    GX_CUDA(cudaMemcpy(e->last_stats.data(), e->d_stats, sizeof(StepStats) * steps, cudaMemcpyDeviceToHost));
+  gx_run_stats rs{};
+  rs.iterations = steps;
+  for (const StepStats& s : e->last_stats) {
+    rs.edges_scanned += static_cast<int64_t>(s.edges);
+    rs.push_iterations += s.mode == MODE_PUSH;
+  }
+  if (steps > 0) {
+    rs.changed_last = static_cast<int64_t>(e->last_stats[steps - 1].changed);
+    rs.residual_l1_last = static_cast<double>(e->last_stats[steps - 1].resid_fx) / c.fx_scale;
+  }
+  rs.ms_total = ms;
+  rs.ms_copy = copy_ms;
+  rs.ms_compute = e->all_resident ? ms : comp_ms;
+  rs.h2d_bytes = h2d_bytes;
+  rs.shards_resident = e->n_resident;
+  rs.shards_streamed = streamed;
+  rs.kernel_launches = launches;
+  rs.pull_launches = pull_launches;
+  rs.ms_pull = ms_pull;
+  if (!e->all_resident && copy_ms > 0 && comp_ms > 0) {
+    const double lo_t = std::min(copy_ms, comp_ms), hi_t = std::max(copy_ms, comp_ms);
+    rs.overlap = std::max(0.0, std::min(1.0, 1.0 - (ms - hi_t) / lo_t));
+  }
+  e->last_run = rs;
+  e->last_app = prm.app;
+  if (out) *out = rs;
+  return GX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void gx_config_default(gx_config* cfg) {
+  if (!cfg) return;
+  cfg->device = 0;
+  cfg->cache_budget_bytes = -1;
+  cfg->stream_slots = 3;
+  cfg->selective_threshold = 0.001;
+  cfg->heavy_degree = 2048;
+  cfg->tile_edges = 2048;
+  cfg->push_sparse = 1;
+  cfg->use_graph = 1;
+  cfg->wait_limit = 1u << 22;
+  cfg->verbose = 0;
+  cfg->profile = 0;
+}
+
+void gx_run_params_default(gx_run_params* p, gx_app app) {
+  if (!p) return;
+  p->app = app;
+  p->max_iter = 10;
+  p->damping = 0.85;
+  p->source = app == GX_APP_SSSP ? 1 : 0;
+  p->weighted = 0;
+  p->tolerance = 0;
+  p->use_init = 0;
+}
+
+gx_status gx_create(const gx_config* cfg, gx_engine** out) {
+  if (!out) return fail(GX_ERR_INVALID, "gx_create: out is NULL");
+  *out = nullptr;
+  gx_config c;
+  gx_config_default(&c);
+  if (cfg) c = *cfg;
+  int n = 0;
+  cudaError_t err = cudaGetDeviceCount(&n);
+  if (err != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return fail(GX_ERR_NODEVICE, "no CUDA device visible (%s)", cudaGetErrorString(err));
+  }
+  if (c.device < 0 || c.device >= n) return fail(GX_ERR_INVALID, "device %d out of range [0,%d)", c.device, n);
+  std::unique_ptr<gx_engine> e(new gx_engine());
+  e->cfg = c;
+  e->dev = c.device;
+  GX_CUDA(cudaSetDevice(e->dev));
+  GX_CUDA(cudaDeviceGetAttribute(&e->n_sm, cudaDevAttrMultiProcessorCount, e->dev));
+  GX_CUDA(cudaStreamCreateWithFlags(&e->s_comp, cudaStreamNonBlocking));
+  GX_CUDA(cudaStreamCreateWithFlags(&e->s_copy, cudaStreamNonBlocking));
+  GX_TRY(alloc_ctl(e.get()));
+  *out = e.release();
+  return GX_OK;
+}
+
+gx_status gx_destroy(gx_engine* e) {
+  if (!e) return GX_OK;
+  delete e;
+  return GX_OK;
+}
+
+gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds, const int64_t* off,
+                      const int32_t* col, const int32_t* outdeg) {
+  if (!e) return fail(GX_ERR_INVALID, "gx_load_csc: engine is NULL");
+  if (V <= 0 || P <= 0 || !bounds || !off || (off[V] > 0 && !col))
+    return fail(GX_ERR_INVALID, "gx_load_csc: bad arguments (V=%d, P=%d)", V, P);
+  if (bounds[0] != 0 || bounds[P] != V) return fail(GX_ERR_INVALID, "gx_load_csc: bounds must run from 0 to V");
+  for (int32_t p = 0; p < P; ++p)
+    if (bounds[p] > bounds[p + 1]) return fail(GX_ERR_INVALID, "gx_load_csc: bounds not monotone at %d", p);
+  if (off[0] != 0) return fail(GX_ERR_INVALID, "gx_load_csc: off[0] must be 0");
+  const int64_t E = off[V];
+  if (E > (int64_t(1) << 40)) return fail(GX_ERR_INVALID, "gx_load_csc: too many edges");
+  for (int32_t v = 0; v < V; ++v)
+    if (off[v] > off[v + 1]) return fail(GX_ERR_INVALID, "gx_load_csc: off not monotone at %d", v);
+  GX_CUDA(cudaSetDevice(e->dev));
+  e->release_graph();
+  e->V = V;
+  e->P = P;
+  e->E = E;
+  e->bounds.assign(bounds, bounds + P + 1);
+  e->off.assign(off, off + V + 1);
+  e->outdeg.assign(V, 0);
+  if (outdeg) {
+    memcpy(e->outdeg.data(), outdeg, sizeof(int32_t) * V);
+  } else {
+    gx_status st = gx_out_degree(V, off, col, e->outdeg.data());
+    if (st != GX_OK) return st;
+  }
+  // Validate source ids once on the host (the kernels index vertex arrays with them).
+  int bad = 0;
+#pragma omp parallel for reduction(| : bad)
+  for (int64_t k = 0; k < E; ++k) bad |= (col[k] < 0 || col[k] >= V);
+  if (bad) return fail(GX_ERR_INVALID, "gx_load_csc: source id outside [0, %d)", V);
+  // Host copy of the edge data (pinned: it is the streaming source when the
+  // budget does not hold every shard).
+  GX_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->h_col), (E + 8) * sizeof(int32_t), cudaHostAllocDefault));
+  memset(e->h_col + E, 0, 8 * sizeof(int32_t));
+#pragma omp parallel for schedule(static)
+  for (int64_t k = 0; k < E; ++k) e->h_col[k] = col[k];
+
+  build_units(e);
+  GX_TRY(dev_alloc(&e->d_off, static_cast<size_t>(V) + 1));
+  GX_CUDA(cudaMemcpy(e->d_off, off, sizeof(int64_t) * (V + 1), cudaMemcpyHostToDevice));
+  GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
+  GX_CUDA(cudaMemcpy(e->d_outdeg, e->outdeg.data(), sizeof(int32_t) * V, cudaMemcpyHostToDevice));
+  for (int i = 0; i < 2; ++i) {
+    uint32_t* vp = nullptr;
+    GX_TRY(dev_alloc(&vp, static_cast<size_t>(V)));
+    e->d_val[i] = vp;
+    GX_TRY(dev_alloc(&e->d_con[i], static_cast<size_t>(V)));
+  }
+  const size_t U = e->units.size();
+  GX_TRY(dev_alloc(&e->d_units, U));
+  GX_TRY(dev_alloc(&e->d_unit_shard, U));
+  if (U) {
+    GX_CUDA(cudaMemcpy(e->d_units, e->units.data(), sizeof(int2) * U, cudaMemcpyHostToDevice));
+    GX_CUDA(cudaMemcpy(e->d_unit_shard, e->unit_shard.data(), sizeof(int32_t) * U, cudaMemcpyHostToDevice));
+  }
+  GX_TRY(dev_alloc(&e->d_heavy, e->heavy.size()));
+  if (!e->heavy.empty())
+    GX_CUDA(cudaMemcpy(e->d_heavy, e->heavy.data(), sizeof(int4) * e->heavy.size(), cudaMemcpyHostToDevice));
+  {
+    uint32_t* pp = nullptr;
+    GX_TRY(dev_alloc(&pp, static_cast<size_t>(e->n_partials)));
+    e->d_partial = pp;
+  }
+  GX_TRY(dev_alloc(&e->d_hticket, e->heavy.size()));
+  e->n_words = (V + 31) / 32 + 2;
+  GX_TRY(dev_alloc(&e->d_bm, static_cast<size_t>(e->n_words)));
+  GX_TRY(dev_alloc(&e->d_frontier, static_cast<size_t>(V)));
+  e->n_work = 2 * P + 2;
+  GX_TRY(dev_alloc(&e->d_work, static_cast<size_t>(e->n_work)));
+  GX_TRY(plan_shards(e));
+  GX_TRY(build_signatures(e));
+  if (e->all_resident) {
+    cudaFreeHost(e->h_col);
+    e->h_col = nullptr;
+  }
+  e->loaded = true;
+  return GX_OK;
+}
+
+gx_status gx_load_shards(gx_engine* e, const char* dir, int32_t V, int32_t P) {
+  if (!e || !dir) return fail(GX_ERR_INVALID, "gx_load_shards: bad arguments");
+  int64_t E = 0;
+  GX_TRY(gx_read_shards(dir, V, P, nullptr, nullptr, nullptr, nullptr, &E));
+  std::vector<int32_t> bounds(P + 1), outdeg(V);
+  std::vector<int64_t> off(static_cast<size_t>(V) + 1);
+  std::vector<int32_t> col(static_cast<size_t>(E) + 1);
+  GX_TRY(gx_read_shards(dir, V, P, bounds.data(), off.data(), col.data(), outdeg.data(), &E));
+  return gx_load_csc(e, V, P, bounds.data(), off.data(), col.data(), outdeg.data());
+}
+
+gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
+  if (!e || !w) return fail(GX_ERR_INVALID, "gx_set_weights: bad arguments");
+  if (!e->loaded) return fail(GX_ERR_STATE, "gx_set_weights: no graph loaded");
+  GX_CUDA(cudaSetDevice(e->dev));
+  if (!e->all_resident && !e->h_col) return fail(GX_ERR_STATE, "gx_set_weights: streaming source missing");
+  if (e->h_w) cudaFreeHost(e->h_w);
+  e->h_w = nullptr;
+  GX_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->h_w), (e->E + 8) * sizeof(uint32_t), cudaHostAllocDefault));
+  memcpy(e->h_w, w, e->E * sizeof(uint32_t));
+  memset(e->h_w + e->E, 0, 8 * sizeof(uint32_t));
+  e->has_weights = true;
+  if (e->all_resident) {
+    // Resident plan with the weights: re-plan against the budget, which now
+    // counts 8 bytes per edge.
+    if (e->cfg.cache_budget_bytes >= 0) {
+      // Need the column data on the host again to re-plan.
+      GX_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->h_col), (e->E + 8) * sizeof(int32_t), cudaHostAllocDefault));
+      GX_CUDA(cudaMemcpy(e->h_col, e->d_col, (e->E + 8) * sizeof(int32_t), cudaMemcpyDeviceToHost));
+      GX_TRY(plan_shards(e));
+      GX_TRY(build_signatures(e));
+      if (e->all_resident) {
+        cudaFreeHost(e->h_col);
+        e->h_col = nullptr;
+      }
+    } else {
+      GX_TRY(dev_alloc(&e->d_w, static_cast<size_t>(e->E) + 8));
+      GX_CUDA(cudaMemset(e->d_w, 0, (e->E + 8) * sizeof(uint32_t)));
+      GX_CUDA(cudaMemcpy(e->d_w, w, e->E * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    }
+  } else {
+    GX_TRY(plan_shards(e));
+  }
+  if (e->all_resident) {
+    cudaFreeHost(e->h_w);
+    e->h_w = nullptr;
+  }
+  e->out_built = false;
+  return GX_OK;
+}
+
+gx_status gx_set_init(gx_engine* e, const void* host_vals) {
+  if (!e || !host_vals) return fail(GX_ERR_INVALID, "gx_set_init: bad arguments");
+  if (!e->loaded) return fail(GX_ERR_STATE, "gx_set_init: no graph loaded");
+  e->init_vals.resize(e->V);
+  memcpy(e->init_vals.data(), host_vals, sizeof(uint32_t) * e->V);
+  e->has_init = true;
+  return GX_OK;
+}
+
+gx_status gx_run(gx_engine* e, const gx_run_params* prm, gx_run_stats* stats) {
+  if (!e || !prm) return fail(GX_ERR_INVALID, "gx_run: bad arguments");
+  if (!e->loaded) return fail(GX_ERR_STATE, "gx_run: no graph loaded");
+  if (prm->max_iter < 0) return fail(GX_ERR_INVALID, "gx_run: max_iter < 0");
+  const int kind = app_kind(*prm);
+  if (kind < 0) return fail(GX_ERR_INVALID, "gx_run: unknown app %d", static_cast<int>(prm->app));
+  if (prm->app == GX_APP_SSSP && (prm->source < 0 || prm->source >= e->V))
+    return fail(GX_ERR_INVALID, "gx_run: SSSP source %d outside [0, %d)", prm->source, e->V);
+  if (kind == K_SSSP_W && !e->has_weights) return fail(GX_ERR_STATE, "gx_run: weighted SSSP needs gx_set_weights");
+  GX_CUDA(cudaSetDevice(e->dev));
+  gx_run_params p = *prm;
+  if (p.max_iter == 0) {
+    e->last_steps = 0;
+    e->last_stats.clear();
+    if (stats) *stats = gx_run_stats{};
+    return GX_OK;
+  }
+  switch (kind) {
+    case K_PR_REF: return run_app<K_PR_REF>(e, p, stats);
+    case K_PR_STD: return run_app<K_PR_STD>(e, p, stats);
+    case K_SSSP_UNIT: return run_app<K_SSSP_UNIT>(e, p, stats);
+    case K_SSSP_W: return run_app<K_SSSP_W>(e, p, stats);
+    case K_CC: return run_app<K_CC>(e, p, stats);
+    case K_INDEG: return run_app<K_INDEG>(e, p, stats);
+  }
+  return fail(GX_ERR_INVALID, "gx_run: unknown app");
+}
+
+gx_status gx_get_values(gx_engine* e, void* host_out) {
+  if (!e || !host_out) return fail(GX_ERR_INVALID, "gx_get_values: bad arguments");
+  if (!e->loaded) return fail(GX_ERR_STATE, "gx_get_values: no graph loaded");
+  GX_CUDA(cudaSetDevice(e->dev));
+  GX_CUDA(cudaMemcpy(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
+  const int cur = e->h_ctl->cur & 1;
+  GX_CUDA(cudaMemcpy(host_out, e->d_val[cur], sizeof(uint32_t) * e->V, cudaMemcpyDeviceToHost));
+  return GX_OK;
+}
+
+gx_status gx_get_iter_stats(gx_engine* e, int32_t step, gx_iter_stats* out) {
+  if (!e || !out) return fail(GX_ERR_INVALID, "gx_get_iter_stats: bad arguments");
+  if (step < 0 || step >= e->last_steps)
+    return fail(GX_ERR_INVALID, "gx_get_iter_stats: step %d outside [0, %d)", step, e->last_steps);
+  const StepStats& s = e->last_stats[step];
+  const double fx = static_cast<double>(e->V) * 1073741824.0;
+  out->changed = static_cast<int64_t>(s.changed);
+  out->active = static_cast<int64_t>(s.active);
+  out->shards_active = s.shards_active < 0 ? e->P : s.shards_active * 1;
+  out->mode = s.mode;
+  out->residual_l1 = static_cast<double>(s.resid_fx) / fx;
+  out->dangling = static_cast<double>(s.dangl_fx) / fx;
+  out->edges_scanned = static_cast<int64_t>(s.edges);
+  return GX_OK;
+}
+
+}  // extern "C"

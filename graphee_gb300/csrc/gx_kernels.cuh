@@ -1,0 +1,598 @@
+// Device kernels of the superstep loop (GraphPS<T>::run,
+// GraphMP/system/GraphPS.h:256-386) for one GB300.
+//
+// One superstep is three launches that read a device control block, so a
+// run of K supersteps can be replayed as one CUDA graph with no host sync:
+//   pull_kernel<APP>      gather-apply over in-edges (CSC) of the swept shards
+//   push_kernel<APP>      sparse min-plus / min-label over out-edges of the frontier
+//   finalize_kernel<APP>  step statistics, frontier compaction, shard activation,
+//                         termination, buffer swap
+// Each kernel returns at once when the control block says the step is not
+// its mode, or that the run is done.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gx {
+
+enum AppKind : int { K_PR_REF = 0, K_PR_STD = 1, K_SSSP_UNIT = 2, K_SSSP_W = 3, K_CC = 4, K_INDEG = 5 };
+enum StepMode : int { MODE_DENSE = 0, MODE_SELECTIVE = 1, MODE_PUSH = 2 };
+
+constexpr int kThreads = 256;           // threads per CTA of pull/push kernels
+constexpr int kWarps = kThreads / 32;
+constexpr int kChunk = 256;             // edges staged per warp per round
+constexpr int kGpsInf = 10000;          // GPS_INF, GraphMP/system/Global.h:50
+constexpr uint32_t kInfW = 0xFFFFFFFFu; // INF of weighted SSSP
+
+struct StepStats {
+  unsigned long long changed;  // reference _Changed_Vertex
+  unsigned long long active;   // |{v : new != old}|
+  unsigned long long edges;    // edges read
+  unsigned long long resid_fx; // PageRank: sum |new-old| in fixed point
+  unsigned long long dangl_fx; // PageRank STD: rank on out-degree-0 vertices, fixed point
+  int shards_active;
+  int mode;
+};
+
+// Control block.  Fields above `step` are set by the host before a run; the
+// rest evolve on the device.
+struct Ctl {
+  int max_iter;
+  int n_vertices;
+  int n_shards;
+  int shard_group;          // shards per bit of the 64-bit shard mask
+  int push_ok;              // out-edges resident: sparse steps may push
+  int pad0;
+  double damping;
+  double inv_n;             // 1.0 / N, as the reference computes it
+  double fx_scale;          // fixed-point scale of resid_fx / dangl_fx
+  double tolerance;         // PageRank L1 stop (0 = off)
+  double sel_threshold;     // BF_THRE
+  // evolving
+  int step;
+  int cur;                  // index of the buffer holding the current values
+  int mode;                 // StepMode of the current step
+  int done;
+  int n_frontier;           // frontier entries for the current push step
+  int error;
+  double base;              // PageRank STD: (1-d)/N + d*D/N of the current step
+  unsigned long long shard_mask;       // active shard groups, current step
+  unsigned long long shard_mask_next;  // being built by finalize
+  unsigned long long changed, active, edges, resid_fx, dangl_fx;  // current-step accumulators
+  unsigned int next_frontier;
+  unsigned int fin_ticket;
+};
+
+struct PullArgs {
+  Ctl* ctl;
+  const int64_t* off;       // global in-edge offsets, V+1
+  const int32_t* col;       // source ids, indexed by global edge id (may be rebased for a streamed shard)
+  const uint32_t* w;        // weights aligned with col (SSSP weighted)
+  const int32_t* outdeg;    // raw out-degree
+  void* val[2];             // T[V] double buffer
+  float* con[2];            // PageRank contributions r[u]/outdeg[u], double buffer
+  const int2* units;        // work units: tile (vb, ve) or heavy chunk (-(h+1), chunk)
+  const int32_t* unit_shard;
+  int32_t u_begin, u_end;   // units of this launch
+  const int4* heavy;        // heavy vertex h: (v, n_chunks, partial base, shard)
+  void* partial;            // per-chunk partial results (T)
+  unsigned int* hticket;    // per heavy vertex: chunks finished this step
+  uint32_t* bm;             // next-frontier bitmap
+};
+
+struct PushArgs {
+  Ctl* ctl;
+  const int64_t* ooff;      // out-edge offsets, V+1
+  const int32_t* ocol;      // destinations
+  const uint32_t* ow;       // weights aligned with ocol
+  void* val[2];
+  const int2* frontier;     // (vertex, value bits) snapshot from the previous step
+  unsigned int* ctr;
+  uint32_t* bm;
+};
+
+struct FinArgs {
+  Ctl* ctl;
+  StepStats* stats;
+  uint32_t* bm;
+  int32_t n_words;
+  const unsigned long long* sig;  // per-vertex 64-bit mask of shard groups it feeds
+  void* val[2];
+  int2* frontier;
+  unsigned int* work_ctr;
+  int32_t n_work_ctr;
+};
+
+template <int APP> struct AppTraits;
+template <> struct AppTraits<K_PR_REF> { typedef float T; };
+template <> struct AppTraits<K_PR_STD> { typedef float T; };
+template <> struct AppTraits<K_SSSP_UNIT> { typedef int32_t T; };
+template <> struct AppTraits<K_SSSP_W> { typedef uint32_t T; };
+template <> struct AppTraits<K_CC> { typedef int32_t T; };
+template <> struct AppTraits<K_INDEG> { typedef int32_t T; };
+
+template <int APP> constexpr bool is_pr() { return APP == K_PR_REF || APP == K_PR_STD; }
+
+__device__ __forceinline__ uint32_t sat_add(uint32_t a, uint32_t b) {
+  uint32_t s = a + b;
+  return s < a ? kInfW : s;
+}
+
+// Candidate an in-edge (u -> v) offers v: PageRank contribution, or the
+// min-plus / min-label candidate.
+template <int APP>
+__device__ __forceinline__ typename AppTraits<APP>::T edge_value(const PullArgs& a, const void* src_val,
+                                                                 const float* src_con, int32_t u, uint32_t wt) {
+  if constexpr (is_pr<APP>()) {
+    return __ldg(src_con + u);
+  } else if constexpr (APP == K_SSSP_UNIT) {
+    return __ldg(static_cast<const int32_t*>(src_val) + u) + 1;  // sssp.cpp:43
+  } else if constexpr (APP == K_SSSP_W) {
+    return sat_add(__ldg(static_cast<const uint32_t*>(src_val) + u), wt);
+  } else {
+    return __ldg(static_cast<const int32_t*>(src_val) + u);      // cc.cpp:42
+  }
+}
+
+template <int APP>
+__device__ __forceinline__ typename AppTraits<APP>::T combine(typename AppTraits<APP>::T acc,
+                                                              typename AppTraits<APP>::T x) {
+  if constexpr (is_pr<APP>()) return acc + x;  // pagerank.cpp:46, ascending edge order
+  else return x < acc ? x : acc;
+}
+
+struct LocalAcc {
+  unsigned long long changed = 0, active = 0, edges = 0, resid = 0, dangl = 0;
+};
+
+// Apply step for vertex v given its gathered value (end of comp_* + end_comp):
+// writes MsgNew[v] (and the next contribution), counts changes.
+template <int APP>
+__device__ __forceinline__ bool apply_vertex(const PullArgs& a, const Ctl& c, int v, typename AppTraits<APP>::T acc,
+                                             typename AppTraits<APP>::T old, void* dst_val, float* dst_con,
+                                             LocalAcc& la) {
+  typedef typename AppTraits<APP>::T T;
+  T nv;
+  if constexpr (APP == K_PR_REF) {
+    // rel = rel*0.85 + 1.0/VertexNum in double, stored as float (pagerank.cpp:48);
+    // explicit _rn ops keep the compiler from contracting into an FMA.
+    nv = static_cast<float>(__dadd_rn(__dmul_rn(static_cast<double>(acc), c.damping), c.inv_n));
+  } else if constexpr (APP == K_PR_STD) {
+    nv = static_cast<float>(__dadd_rn(c.base, __dmul_rn(c.damping, static_cast<double>(acc))));
+  } else {
+    nv = acc;
+  }
+  static_cast<T*>(dst_val)[v] = nv;
+  if constexpr (is_pr<APP>()) {
+    const int32_t od = __ldg(a.outdeg + v);
+    dst_con[v] = nv / static_cast<float>(od > 0 ? od : 1);  // Msg[u]/_VertexOut[u], clamp pagerank.cpp:77-80
+    const double diff = fabs(static_cast<double>(nv) - static_cast<double>(old));
+    la.resid += __double2ull_rn(diff * c.fx_scale);
+    if (APP == K_PR_STD && od == 0) la.dangl += __double2ull_rn(static_cast<double>(nv) * c.fx_scale);
+  }
+  // _Changed_Vertex counts new != VertexValue; VertexValue is 0 before the
+  // first step and equals Msg afterwards (pagerank.cpp:56-59, GraphPS.h:338-345).
+  const T prev = c.step == 0 ? T(0) : old;
+  la.changed += (nv != prev);
+  const bool act = nv != old;
+  la.active += act;  // not reported from here; finalize recounts from the bitmap
+  return act;
+}
+
+__device__ __forceinline__ void bitmap_set_tile(uint32_t* bm, int vb, unsigned mask) {
+  // Lanes are consecutive vertices vb..vb+31: at most two bitmap words.
+  if (mask == 0) return;
+  const int sh = vb & 31;
+  const int w0 = vb >> 5;
+  const unsigned lo = mask << sh;
+  const unsigned hi = sh ? (mask >> (32 - sh)) : 0u;
+  if (lo) atomicOr(bm + w0, lo);
+  if (hi) atomicOr(bm + w0 + 1, hi);
+}
+
+__device__ __forceinline__ unsigned long long warp_sum(unsigned long long x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+// ---------------------------------------------------------------------------
+// Pull.  The swept vertices are cut into warp-sized work units with bounded
+// edge counts, assigned to warps round-robin (no global work counter):
+//  * a tile of up to 32 consecutive light vertices stages its contiguous edge
+//    range through shared memory (128-bit streaming index loads, one gather
+//    per edge); each lane then folds its own vertex's edges in ascending edge
+//    order, which is the reference's summation order (pagerank.cpp:44-47);
+//  * a heavy vertex is split into chunks of kHeavyChunk edges; each chunk is
+//    reduced by one warp in a fixed lane pattern, and the warp that finishes
+//    the last chunk folds the per-chunk partials in chunk order and applies
+//    the vertex.  Results are deterministic run to run.
+// ---------------------------------------------------------------------------
+constexpr int kHeavyChunk = 4096;
+
+template <int APP>
+__device__ __forceinline__ typename AppTraits<APP>::T identity() {
+  typedef typename AppTraits<APP>::T T;
+  if constexpr (is_pr<APP>()) return T(0);
+  else if constexpr (APP == K_SSSP_W) return kInfW;
+  else return T(0x7fffffff);
+}
+
+__device__ __forceinline__ void flush_block(Ctl* ctl, const LocalAcc& la) {
+  __shared__ unsigned long long s_red[4][kWarps];
+  unsigned long long ch = warp_sum(la.changed), ed = warp_sum(la.edges), rs = warp_sum(la.resid),
+                     dg = warp_sum(la.dangl);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    s_red[0][wid] = ch;
+    s_red[1][wid] = ed;
+    s_red[2][wid] = rs;
+    s_red[3][wid] = dg;
+  }
+  __syncthreads();
+  if (threadIdx.x < 4) {
+    unsigned long long t = 0;
+    for (int i = 0; i < kWarps; ++i) t += s_red[threadIdx.x][i];
+    unsigned long long* dst = threadIdx.x == 0 ? &ctl->changed
+                            : threadIdx.x == 1 ? &ctl->edges
+                            : threadIdx.x == 2 ? &ctl->resid_fx
+                                               : &ctl->dangl_fx;
+    if (t) atomicAdd(dst, t);
+  }
+}
+
+template <int APP>
+__global__ void __launch_bounds__(kThreads) pull_kernel(PullArgs a) {
+  typedef typename AppTraits<APP>::T T;
+  __shared__ T s_buf[kWarps][kChunk];
+  Ctl* ctl = a.ctl;
+  const int done = ctl->done, mode = ctl->mode;
+  if (done || mode == MODE_PUSH) return;
+  Ctl c;
+  c.step = ctl->step;
+  c.damping = ctl->damping;
+  c.inv_n = ctl->inv_n;
+  c.fx_scale = ctl->fx_scale;
+  c.base = ctl->base;
+  const int cur = ctl->cur;
+  const int group = ctl->shard_group;
+  const unsigned long long smask = ctl->shard_mask;
+  const void* src_val = a.val[cur];
+  void* dst_val = a.val[cur ^ 1];
+  const float* src_con = a.con[cur];
+  float* dst_con = a.con[cur ^ 1];
+  const bool selective = mode == MODE_SELECTIVE;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int gw = blockIdx.x * kWarps + wid;
+  const int nw = gridDim.x * kWarps;
+  T* buf = s_buf[wid];
+  LocalAcc la;
+
+  for (int u = a.u_begin + gw; u < a.u_end; u += nw) {
+    const int2 wu = a.units[u];
+    const bool on = !selective || ((smask >> (a.unit_shard[u] / group)) & 1ull);
+    if (wu.x < 0) {
+      // ---- heavy chunk ----
+      const int h = -wu.x - 1;
+      const int4 H = a.heavy[h];
+      const int v = H.x;
+      if (!on) {
+        if (wu.y == 0 && lane == 0) {
+          static_cast<T*>(dst_val)[v] = static_cast<const T*>(src_val)[v];
+          if constexpr (is_pr<APP>()) dst_con[v] = src_con[v];
+        }
+        continue;
+      }
+      const int64_t vb = a.off[v], ve = a.off[v + 1];
+      const int64_t b = vb + static_cast<int64_t>(wu.y) * kHeavyChunk;
+      const int64_t e = ve < b + kHeavyChunk ? ve : b + kHeavyChunk;
+      T acc = identity<APP>();
+      if constexpr (APP != K_INDEG) {
+        for (int64_t q = (b & ~3ll) + 4 * lane; q < e; q += 256) {
+          const int64_t q2 = q + 128;
+          const int4 c4 = __ldcs(reinterpret_cast<const int4*>(a.col + q));
+          int4 d4 = make_int4(0, 0, 0, 0);
+          if (q2 < e) d4 = __ldcs(reinterpret_cast<const int4*>(a.col + q2));
+          uint4 w4 = make_uint4(0, 0, 0, 0), x4 = make_uint4(0, 0, 0, 0);
+          if constexpr (APP == K_SSSP_W) {
+            w4 = __ldcs(reinterpret_cast<const uint4*>(a.w + q));
+            if (q2 < e) x4 = __ldcs(reinterpret_cast<const uint4*>(a.w + q2));
+          }
+          const int cs[8] = {c4.x, c4.y, c4.z, c4.w, d4.x, d4.y, d4.z, d4.w};
+          const uint32_t ws[8] = {w4.x, w4.y, w4.z, w4.w, x4.x, x4.y, x4.z, x4.w};
+          T vals[8];
+#pragma unroll
+          for (int j = 0; j < 8; ++j) {
+            const int64_t k = (j < 4 ? q : q2) + (j & 3);
+            vals[j] = (k >= b && k < e) ? edge_value<APP>(a, src_val, src_con, cs[j], ws[j]) : identity<APP>();
+          }
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc = combine<APP>(acc, vals[j]);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc = combine<APP>(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+      }
+      if (lane == 0) {
+        la.edges += e - b;
+        T* part = static_cast<T*>(a.partial);
+        part[H.z + wu.y] = acc;
+        __threadfence();
+        const unsigned t = atomicAdd(a.hticket + h, 1u);
+        if (t == static_cast<unsigned>(H.y) - 1) {
+          __threadfence();
+          const volatile T* vp = part;
+          T tot = identity<APP>();
+          for (int i = 0; i < H.y; ++i) tot = combine<APP>(tot, vp[H.z + i]);
+          const T old = static_cast<const T*>(src_val)[v];
+          T fin;
+          if constexpr (is_pr<APP>()) fin = tot;
+          else if constexpr (APP == K_INDEG) fin = static_cast<T>(ve - vb);
+          else fin = combine<APP>(old, tot);
+          if (apply_vertex<APP>(a, c, v, fin, old, dst_val, dst_con, la)) atomicOr(a.bm + (v >> 5), 1u << (v & 31));
+          a.hticket[h] = 0;
+        }
+      }
+      continue;
+    }
+    // ---- tile of light vertices ----
+    const int vb = wu.x, n = wu.y - wu.x;
+    const bool valid = lane < n;
+    const int v = vb + lane;
+    int64_t beg = 0, end = 0;
+    T old = T(0);
+    if (valid) {
+      beg = a.off[v];
+      end = a.off[v + 1];
+      old = __ldcs(static_cast<const T*>(src_val) + v);
+    }
+    if (!on) {
+      if (valid) {
+        static_cast<T*>(dst_val)[v] = old;
+        if constexpr (is_pr<APP>()) dst_con[v] = src_con[v];
+      }
+      continue;
+    }
+    const int64_t E0 = __shfl_sync(0xffffffffu, beg, 0);
+    const int64_t E1 = __shfl_sync(0xffffffffu, end, n - 1);
+    T acc;
+    if constexpr (is_pr<APP>()) acc = 0.f;
+    else acc = old;
+    if constexpr (APP != K_INDEG) {
+      for (int64_t c0 = E0 & ~3ll; c0 < E1; c0 += kChunk) {
+#pragma unroll
+        for (int j = 0; j < kChunk / 128; ++j) {
+          const int64_t q = c0 + 4 * (lane + 32 * j);
+          if (q < E1) {
+            const int4 c4 = __ldcs(reinterpret_cast<const int4*>(a.col + q));
+            uint4 w4 = make_uint4(0, 0, 0, 0);
+            if constexpr (APP == K_SSSP_W) w4 = __ldcs(reinterpret_cast<const uint4*>(a.w + q));
+            const int cs[4] = {c4.x, c4.y, c4.z, c4.w};
+            const uint32_t ws[4] = {w4.x, w4.y, w4.z, w4.w};
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const int64_t k = q + e;
+              if (k >= E0 && k < E1) buf[4 * (lane + 32 * j) + e] = edge_value<APP>(a, src_val, src_con, cs[e], ws[e]);
+            }
+          }
+        }
+        __syncwarp();
+        const int64_t lo = beg > c0 ? beg : c0;
+        const int64_t hi = end < c0 + kChunk ? end : c0 + kChunk;
+        for (int64_t k = lo; k < hi; ++k) acc = combine<APP>(acc, buf[k - c0]);
+        __syncwarp();
+      }
+    } else {
+      acc = static_cast<T>(end - beg);
+    }
+    bool act = false;
+    if (valid) {
+      la.edges += end - beg;
+      act = apply_vertex<APP>(a, c, v, acc, old, dst_val, dst_con, la);
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, act);
+    if (lane == 0) bitmap_set_tile(a.bm, vb, m);
+  }
+  flush_block(ctl, la);
+}
+
+// ---------------------------------------------------------------------------
+// Push (sparse steps of SSSP/CC): each frontier vertex u, with the value it
+// held at the end of the previous step, relaxes its out-edges with atomicMin.
+// For min-plus / min-label this equals the Jacobi pull of the reference:
+// a vertex whose in-neighbours did not change cannot improve.
+// ---------------------------------------------------------------------------
+template <int APP>
+__global__ void __launch_bounds__(kThreads) push_kernel(PushArgs a) {
+  typedef typename AppTraits<APP>::T T;
+  if (a.ctl->done || a.ctl->mode != MODE_PUSH) return;
+  const int cur = a.ctl->cur;
+  const int lane = threadIdx.x & 31;
+  const int nf = a.ctl->n_frontier;
+  LocalAcc la;
+  if constexpr (!is_pr<APP>() && APP != K_INDEG) {
+  T* val = static_cast<T*>(a.val[cur]);
+  for (;;) {
+    int base = 0;
+    if (lane == 0) base = static_cast<int>(atomicAdd(a.ctr, 32u));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= nf) break;
+    const int cnt = nf - base < 32 ? nf - base : 32;
+    int2 my = make_int2(0, 0);
+    if (lane < cnt) my = a.frontier[base + lane];
+    for (int j = 0; j < cnt; ++j) {
+      const int u = __shfl_sync(0xffffffffu, my.x, j);
+      const T su = static_cast<T>(__shfl_sync(0xffffffffu, my.y, j));
+      const int64_t b = a.ooff[u], e = a.ooff[u + 1];
+      if (lane == 0) la.edges += e - b;
+      for (int64_t k = b + lane; k < e; k += 32) {
+        const int vtx = __ldcs(a.ocol + k);
+        T cand;
+        if constexpr (APP == K_SSSP_UNIT) cand = su + 1;
+        else if constexpr (APP == K_SSSP_W) cand = sat_add(static_cast<uint32_t>(su), __ldcs(a.ow + k));
+        else cand = su;
+        if (cand < val[vtx]) {
+          const T prev = atomicMin(val + vtx, cand);
+          if (cand < prev) {
+            const uint32_t bit = 1u << (vtx & 31);
+            const uint32_t was = atomicOr(a.bm + (vtx >> 5), bit);
+            if (!(was & bit)) la.changed += 1;
+          }
+        }
+      }
+    }
+  }
+  }
+  flush_block(a.ctl, la);
+}
+
+// ---------------------------------------------------------------------------
+// Finalize: the host-side tail of GraphPS::run's step (GraphPS.h:291-385) on
+// the device.  All CTAs sweep the next-frontier bitmap: count it, clear it,
+// and — when the next step is selective — either compact it into the push
+// frontier or OR the shard-group masks of its vertices into the next shard
+// mask (the bloom-filter partition test of GraphPS.h:349-368, made exact per
+// shard group).  The last CTA to finish records the step and advances.
+// ---------------------------------------------------------------------------
+template <int APP>
+__global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
+  typedef typename AppTraits<APP>::T T;
+  __shared__ unsigned long long s_act[kWarps];
+  __shared__ unsigned long long s_mask[kWarps];
+  __shared__ bool s_last;
+  Ctl* ctl = a.ctl;
+  const Ctl c = *ctl;
+  if (c.done) return;
+  // updated_ratio is a float in the reference (GraphPS.h:203,297).
+  const float ratio = static_cast<float>(static_cast<double>(c.changed) / c.n_vertices);
+  const bool sel_next = static_cast<double>(ratio) < c.sel_threshold;
+  const bool push_next = sel_next && c.push_ok;
+  const bool want_mask = sel_next && !push_next && a.sig != nullptr;
+  const T* newv = static_cast<const T*>(a.val[c.mode == MODE_PUSH ? c.cur : (c.cur ^ 1)]);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  unsigned long long act = 0, mask = 0;
+  for (int w = blockIdx.x * kThreads + threadIdx.x; w < a.n_words; w += gridDim.x * kThreads) {
+    uint32_t word = a.bm[w];
+    if (!word) continue;
+    a.bm[w] = 0;
+    act += __popc(word);
+    if (want_mask) {
+      for (uint32_t x = word; x; x &= x - 1) mask |= a.sig[(w << 5) + __ffs(x) - 1];
+    }
+    if (push_next) {
+      for (uint32_t x = word; x; x &= x - 1) {
+        const int u = (w << 5) + __ffs(x) - 1;
+        const unsigned pos = atomicAdd(&ctl->next_frontier, 1u);
+        T vu = newv[u];
+        a.frontier[pos] = make_int2(u, *reinterpret_cast<int*>(&vu));
+      }
+    }
+  }
+  act = warp_sum(act);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mask |= __shfl_xor_sync(0xffffffffu, mask, o);
+  if (lane == 0) {
+    s_act[wid] = act;
+    s_mask[wid] = mask;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned long long ta = 0, tm = 0;
+    for (int i = 0; i < kWarps; ++i) {
+      ta += s_act[i];
+      tm |= s_mask[i];
+    }
+    if (ta) atomicAdd(&ctl->active, ta);
+    if (tm) atomicOr(&ctl->shard_mask_next, tm);
+    __threadfence();
+    const unsigned ticket = atomicAdd(&ctl->fin_ticket, 1u);
+    s_last = ticket == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!s_last) return;
+  __threadfence();
+  if (threadIdx.x == 0) {
+    volatile Ctl* vc = ctl;
+    StepStats s;
+    s.changed = vc->changed;
+    s.active = vc->active;
+    s.edges = vc->edges;
+    s.resid_fx = vc->resid_fx;
+    s.dangl_fx = vc->dangl_fx;
+    s.mode = c.mode;
+    s.shards_active = c.mode == MODE_SELECTIVE ? __popcll(c.shard_mask) : -1;
+    a.stats[c.step] = s;
+    const unsigned long long next_mask = vc->shard_mask_next;
+    const double resid = static_cast<double>(s.resid_fx) / c.fx_scale;
+    int done = (s.changed == 0 && c.step > 1) || (c.step + 1 >= c.max_iter);  // GraphPS.h:256,383
+    if (is_pr<APP>() && c.tolerance > 0 && resid < c.tolerance) done = 1;
+    ctl->cur = c.mode == MODE_PUSH ? c.cur : (c.cur ^ 1);  // Msg <- MsgNew as a swap
+    ctl->mode = push_next ? MODE_PUSH : (sel_next ? MODE_SELECTIVE : MODE_DENSE);
+    ctl->shard_mask = want_mask ? next_mask : ~0ull;
+    ctl->shard_mask_next = 0;
+    ctl->n_frontier = static_cast<int>(vc->next_frontier);
+    ctl->next_frontier = 0;
+    if (APP == K_PR_STD) {
+      const double D = static_cast<double>(s.dangl_fx) / c.fx_scale;
+      ctl->base = (1.0 - c.damping) * c.inv_n + c.damping * D * c.inv_n;
+    }
+    ctl->changed = 0;
+    ctl->active = 0;
+    ctl->edges = 0;
+    ctl->resid_fx = 0;
+    ctl->dangl_fx = 0;
+    ctl->fin_ticket = 0;
+    ctl->step = c.step + 1;
+    __threadfence();
+    ctl->done = done;
+  }
+  for (int i = threadIdx.x; i < a.n_work_ctr; i += kThreads) a.work_ctr[i] = 0;
+}
+
+// Initial values (init_vertex of each app) and PageRank contributions.
+template <int APP>
+__global__ void init_kernel(Ctl* ctl, void* val, float* con, const int32_t* outdeg, int n, int source, int use_init) {
+  typedef typename AppTraits<APP>::T T;
+  T* v = static_cast<T*>(val);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (!use_init) {
+      if constexpr (is_pr<APP>()) v[i] = static_cast<float>(ctl->inv_n);  // assign(V, 1.0/V), pagerank.cpp:81
+      else if constexpr (APP == K_SSSP_UNIT) v[i] = i == source ? 0 : kGpsInf;  // sssp.cpp:70-72
+      else if constexpr (APP == K_SSSP_W) v[i] = i == source ? 0u : kInfW;
+      else if constexpr (APP == K_CC) v[i] = i;  // cc.cpp:70-73
+      else v[i] = 0;  // cal.cpp:77
+    }
+    if constexpr (is_pr<APP>()) {
+      const int32_t od = outdeg[i];
+      con[i] = v[i] / static_cast<float>(od > 0 ? od : 1);
+    }
+  }
+}
+
+// Per-vertex shard-group masks: bit g of sig[u] is set iff u is a source in
+// a shard of group g.  Replaces the bloom-filter build (GraphPS.h:225-245).
+__global__ void signature_kernel(unsigned long long* sig, const int32_t* col, int64_t e0, int64_t e1,
+                                 unsigned long long bit) {
+  for (int64_t k = e0 + blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < e1;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    const int u = col[k];
+    if ((sig[u] & bit) == 0) atomicOr(sig + u, bit);
+  }
+}
+
+// Out-edge CSR from the CSC (counting sort by source; order within a source
+// is unspecified, which min-plus / min-label do not observe).
+__global__ void transpose_kernel(const int64_t* off, const int32_t* col, const uint32_t* w, int n,
+                                 unsigned long long* cursor, int32_t* ocol, uint32_t* ow) {
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
+    for (int64_t k = off[v] + lane; k < off[v + 1]; k += 32) {
+      const int u = col[k];
+      const unsigned long long p = atomicAdd(cursor + u, 1ull);
+      ocol[p] = v;
+      if (w) ow[p] = w[k];
+    }
+  }
+}
+
+}  // namespace gx

@@ -1,0 +1,194 @@
+/*
+ * gx.h — C ABI of the GB300-native GraphMP hot path.
+ *
+ * The reference's operator interface is a C++ template engine,
+ * GraphPS<T> (GraphMP/system/GraphPS.h:22-63), driven as
+ *   init(path, V, P, maxIter)   (GraphPS.h:77)
+ *   run()                       (GraphPS.h:171)
+ * with a vertex program plugged in through the function pointer _comp
+ * (GraphPS.h:25-34) and the virtual init_vertex() (GraphPS.h:60).  This ABI
+ * replaces that engine: the shard files, vertex arrays, vertex programs and
+ * termination rule are the reference's, the execution is CUDA on one GB300.
+ * Every function returns gx_status; no C++ exception crosses this boundary;
+ * gx_last_error() returns a thread-local message for the last failure.
+ *
+ * Plain pointers and sizes only.  Host pointers unless a parameter says
+ * "device".  One gx_engine per host thread.
+ */
+#ifndef GX_H_
+#define GX_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum gx_status {
+  GX_OK = 0,
+  GX_ERR_INVALID = 1,  /* bad argument */
+  GX_ERR_IO = 2,       /* file missing / short read (reference: abort(), cnpy.h:131-134) */
+  GX_ERR_FORMAT = 3,   /* shard header or .npy header mismatch */
+  GX_ERR_OOM = 4,      /* device or pinned allocation failed */
+  GX_ERR_CUDA = 5,     /* CUDA runtime error */
+  GX_ERR_TIMEOUT = 6,  /* a bounded device-side wait gave up */
+  GX_ERR_NODEVICE = 7, /* no CUDA device visible */
+  GX_ERR_STATE = 8     /* call out of order (e.g. run before load) */
+} gx_status;
+
+/* Vertex programs.  GraphMP binds these through GraphPS<T>::_comp. */
+typedef enum gx_app {
+  /* comp_pagerank<float> (GraphMP/app/pagerank.cpp:20-84): FP32 pull sum of
+   * Msg[u]/outdeg[u] (outdeg clamped to >=1), new = (double)acc*0.85 + 1.0/N
+   * stored as float, init 1/N, dangling mass dropped. */
+  GX_APP_PAGERANK_REF = 0,
+  /* Standard PageRank: r' = (1-d)/N + d*(sum r[u]/outdeg[u] + D/N) with D the
+   * rank held by vertices of out-degree 0.  No reference counterpart. */
+  GX_APP_PAGERANK_STD = 1,
+  /* comp_sssp<int32_t> (GraphMP/app/sssp.cpp:20-75): pull min-plus.  Unit
+   * weights with INF = GPS_INF = 10000 (GraphMP/system/Global.h:50), or
+   * uint32 weights with INF = 0xFFFFFFFF and saturating add. */
+  GX_APP_SSSP = 2,
+  /* comp_cc<int32_t> (GraphMP/app/cc.cpp:20-75): pull min-label, init l[v]=v. */
+  GX_APP_CC = 3,
+  /* comp_pagerank in GraphMP/app/cal.cpp:20-58: value = in-degree. */
+  GX_APP_INDEGREE = 4
+} gx_app;
+
+typedef struct gx_engine gx_engine;
+
+typedef struct gx_config {
+  int32_t device;              /* CUDA device ordinal (default 0) */
+  int64_t cache_budget_bytes;  /* HBM shard-cache budget for edge data; <0 = unlimited.
+                                  Replaces EDGE_CACHE_SIZE (GraphMP/system/Global.h:52). */
+  int32_t stream_slots;        /* device slots in the streaming ring (>=2, default 3) */
+  double selective_threshold;  /* BF_THRE (GraphMP/system/Global.h:57), default 0.001 */
+  int32_t heavy_degree;        /* in-degree above which a vertex gets a whole CTA (default 2048) */
+  int32_t tile_edges;          /* edge cap of one warp tile (default 2048) */
+  int32_t push_sparse;         /* SSSP/CC: push over out-edges when selective (default 1) */
+  int32_t use_graph;           /* replay the iteration loop as a CUDA graph (default 1) */
+  uint32_t wait_limit;         /* iteration cap of every device spin-wait (default 1<<22) */
+  int32_t verbose;             /* per-iteration log lines on stderr (default 0) */
+  int32_t profile;             /* time every pull launch with CUDA events (default 0) */
+} gx_config;
+
+typedef struct gx_run_params {
+  gx_app app;
+  int32_t max_iter;      /* reference: GraphPS::init's MaxIteration */
+  double damping;        /* PageRank d, default 0.85 (pagerank.cpp:48) */
+  int32_t source;        /* SSSP source vertex (reference hard-codes 1, sssp.cpp:72) */
+  int32_t weighted;      /* SSSP: 1 = weights from gx_set_weights, 0 = unit weight */
+  double tolerance;      /* PageRank: also stop once the L1 residual < tolerance (0 = off) */
+  int32_t use_init;      /* 1 = start from gx_set_init values instead of the app's init_vertex */
+} gx_run_params;
+
+typedef struct gx_run_stats {
+  int32_t iterations;       /* supersteps executed (reference: `step` at exit) */
+  int32_t push_iterations;  /* of those, sparse push supersteps */
+  int64_t changed_last;     /* _Changed_Vertex of the last step */
+  double residual_l1_last;  /* PageRank: sum |new-old| of the last step */
+  int64_t edges_scanned;    /* edges read over all steps */
+  double ms_total;          /* wall time of gx_run's superstep loop (device events) */
+  double ms_copy;           /* streamed-shard H2D time (copy stream busy time) */
+  double ms_compute;        /* compute stream busy time */
+  double overlap;           /* copy/compute overlap fraction (streamed runs) */
+  int64_t h2d_bytes;        /* shard bytes streamed from pinned host memory */
+  int32_t shards_resident;  /* shards held in the HBM shard cache */
+  int32_t shards_streamed;  /* shard visits served by the streaming ring */
+  int32_t kernel_launches;  /* device kernels launched by this run */
+  int32_t pull_launches;    /* of those, pull kernels of executed steps */
+  double ms_pull;           /* summed pull-kernel time (config.profile only) */
+} gx_run_stats;
+
+typedef struct gx_iter_stats {
+  int64_t changed;        /* reference _Changed_Vertex: computed value != previous value */
+  int64_t active;         /* |{v : MsgNew[v] != Msg[v]}| (next frontier) */
+  int32_t shards_active;  /* shards swept this step */
+  int32_t mode;           /* 0 dense pull, 1 selective pull, 2 push */
+  double residual_l1;     /* PageRank: sum |new-old| */
+  double dangling;        /* PageRank STD: dangling mass D used by the NEXT step */
+  int64_t edges_scanned;
+} gx_iter_stats;
+
+/* ---- engine (replaces GraphPS<T>, GraphMP/system/GraphPS.h:22-387) ---- */
+
+void gx_config_default(gx_config* cfg);
+void gx_run_params_default(gx_run_params* p, gx_app app);
+const char* gx_last_error(void);
+
+gx_status gx_create(const gx_config* cfg, gx_engine** out);
+gx_status gx_destroy(gx_engine* e);
+
+/* Loads the reference's shard directory: {p}.edge.npy for p in [0,P), each a
+ * 1-D int32 .npy of [E_p, len(indices), len(indptr), start, end, indices...,
+ * indptr...] (GraphMP/system/Comp.h:33-42, written by
+ * GraphMP/tools/format_spark.py:148-154), and vertexout.npy (int32[V],
+ * GraphPS.h:162-169).  `dir` ends with '/', as GraphPS::init expects.
+ * Replaces GraphPS::init (GraphPS.h:77-151) + load_edge (Global.h:129-255). */
+gx_status gx_load_shards(gx_engine* e, const char* dir, int32_t V, int32_t P);
+
+/* Loads an in-memory graph in the same shard layout, as one global CSC:
+ * bounds[P+1] destination ranges, off[V+1] in-edge offsets, col[off[V]]
+ * source ids, outdeg[V] (NULL = computed from col). */
+gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
+                      const int64_t* off, const int32_t* col, const int32_t* outdeg);
+
+/* SSSP edge weights aligned with col (uint32, >= 1). */
+gx_status gx_set_weights(gx_engine* e, const uint32_t* w);
+
+/* Initial vertex values (T[V]: float for PageRank, int32 for SSSP/CC);
+ * the init_vertex() override (GraphPS.h:60). Used when params.use_init. */
+gx_status gx_set_init(gx_engine* e, const void* host_vals);
+
+/* Superstep loop of GraphPS<T>::run (GraphPS.h:256-386). */
+gx_status gx_run(gx_engine* e, const gx_run_params* params, gx_run_stats* stats);
+
+/* Copies the final _VertexMsg (T[V]) to host memory. */
+gx_status gx_get_values(gx_engine* e, void* host_out);
+
+/* Per-step statistics of the last gx_run (the reference logs these per
+ * iteration, GraphPS.h:375-382). */
+gx_status gx_get_iter_stats(gx_engine* e, int32_t step, gx_iter_stats* out);
+
+/* ---- graph construction and the reference's on-disk format (host) ---- */
+
+enum { GX_BUILD_DROP_SELF = 1, GX_BUILD_DEDUP = 2, GX_BUILD_SYMMETRIZE = 4 };
+
+/* Seeded R-MAT edge list: n edges over 2^scale vertices, quadrant
+ * probabilities a, b, c (d = 1-a-b-c).  Edge i is a pure function of
+ * (seed, i), so any range of edges can be generated independently. */
+gx_status gx_rmat_edges(int32_t scale, int64_t n, double a, double b, double c,
+                        uint64_t seed, int64_t first, int32_t* src, int32_t* dst);
+
+/* Builds the CSC (in-edges grouped by destination, sources ascending) of an
+ * edge list.  col must hold n entries (2n with GX_BUILD_SYMMETRIZE).
+ * *n_out receives off[V]. */
+gx_status gx_build_csc(int32_t V, int64_t n, const int32_t* src, const int32_t* dst,
+                       int32_t flags, int64_t* off, int32_t* col, int64_t* n_out);
+
+/* Edge-balanced destination-range shard boundaries, the rule of
+ * GraphMP/tools/format_spark.py:91-108: bounds[i] = first v with
+ * off[v] >= ceil(E/P)*i, bounds[0] = 0, bounds[P] = V. */
+gx_status gx_partition_bounds(int32_t V, const int64_t* off, int32_t P, int32_t* bounds);
+
+/* outdeg[u] = number of CSC entries with source u. */
+gx_status gx_out_degree(int32_t V, const int64_t* off, const int32_t* col, int32_t* outdeg);
+
+/* Writes {p}.edge.npy, vertexout.npy and vertexin.npy in the reference layout. */
+gx_status gx_write_shards(const char* dir, int32_t V, int32_t P, const int32_t* bounds,
+                          const int64_t* off, const int32_t* col, const int32_t* outdeg);
+
+/* Reads a shard directory into a global CSC (the host half of gx_load_shards).
+ * Call first with off/col NULL to get *E_out; then with buffers. */
+gx_status gx_read_shards(const char* dir, int32_t V, int32_t P, int32_t* bounds,
+                         int64_t* off, int32_t* col, int32_t* outdeg, int64_t* E_out);
+
+/* Seeded SSSP weights in [1,255], a pure function of (seed, u, v). */
+gx_status gx_edge_weights(uint64_t seed, int32_t V, const int64_t* off, const int32_t* col,
+                          uint32_t* w);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GX_H_ */

@@ -1,0 +1,51 @@
+"""The C-ABI library loads on a machine without a GPU and exports every
+function include/gx.h declares; host-only entry points work; engine entry
+points report errors instead of crashing when no device is visible."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+import graphee_gb300 as gx
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_functions():
+    names = set()
+    for h in sorted((ROOT / "include").glob("*.h")):
+        text = h.read_text()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(gx_\w+)\s*\(", text, flags=re.M))
+    return sorted(names)
+
+
+def test_header_declares_functions():
+    names = declared_functions()
+    assert "gx_run" in names and "gx_load_shards" in names and len(names) >= 15
+
+
+def test_library_exports_every_declared_symbol():
+    L = gx.lib()
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_config_defaults():
+    cfg = gx.default_config()
+    assert cfg.cache_budget_bytes == -1
+    assert cfg.selective_threshold == pytest.approx(0.001)   # BF_THRE
+    assert cfg.stream_slots >= 2
+    p = gx.RunParams()
+    gx.lib().gx_run_params_default(C.byref(p), gx.APP_SSSP)
+    assert p.source == 1 and p.damping == pytest.approx(0.85)
+
+
+def test_null_arguments_are_errors():
+    L = gx.lib()
+    assert L.gx_create(None, None) == gx.GX_ERR_INVALID
+    assert L.gx_run(None, None, None) == gx.GX_ERR_INVALID
+    assert L.gx_get_values(None, None) == gx.GX_ERR_INVALID
+    assert "bad arguments" in L.gx_last_error().decode()
+    assert L.gx_destroy(None) == gx.GX_OK

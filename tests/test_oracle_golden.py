@@ -1,0 +1,103 @@
+"""Pins the oracle (oracle/gx_oracle.cpp) against the reference's own app
+outputs (tests/golden/, made by tests/golden/make_golden.py from the
+reference's GraphMP apps): values bit for bit, and the per-iteration
+`Update` counts of GraphPS::run's log line."""
+import numpy as np
+import pytest
+
+import gx_oracle as O
+
+
+@pytest.mark.parametrize("threads", [1, 4])
+def test_pagerank_bitexact_vs_reference(golden_cases, threads):
+    for name, g in golden_cases.items():
+        vals, changed, _ = O.run(O.PAGERANK_REF, int(g["V"]), int(g["P"]), g["bounds"], g["off"], g["col"],
+                                 g["outdeg"], 20, threads=threads)
+        assert vals.dtype == np.float32
+        assert np.array_equal(vals.view(np.uint32), g["pr"].view(np.uint32)), name
+        assert np.array_equal(changed, g["pr_changed"]), name
+
+
+@pytest.mark.parametrize("source", [1, 0])
+def test_sssp_unit_vs_reference(golden_cases, source):
+    for name, g in golden_cases.items():
+        vals, changed, _ = O.run(O.SSSP, int(g["V"]), int(g["P"]), g["bounds"], g["off"], g["col"], g["outdeg"],
+                                 200, source=source)
+        assert np.array_equal(vals, g[f"sssp{source}"]), name
+        assert np.array_equal(changed, g[f"sssp{source}_changed"]), name
+
+
+def test_cc_vs_reference(golden_cases):
+    for name, g in golden_cases.items():
+        vals, changed, _ = O.run(O.CC, int(g["V"]), int(g["P"]), g["bounds"], g["off"], g["col"], g["outdeg"], 200)
+        assert np.array_equal(vals, g["cc"]), name
+        assert np.array_equal(changed, g["cc_changed"]), name
+
+
+def test_pagerank_fp64_error_bound(golden_cases):
+    """On R-MAT graphs the reference's FP32 ranks stay within 1e-5 relative of
+    the same formula in FP64, the yardstick for the GPU's tolerance.  The hub
+    fixture (3000 equal in-contributions summed in order) is the known
+    exception: the reference's own sequential FP32 sum is ~2e-4 off there,
+    which is why exact-order mode exists for bit-exact parity."""
+    for name, g in golden_cases.items():
+        v64, _, _ = O.run(O.PAGERANK_REF64, int(g["V"]), int(g["P"]), g["bounds"], g["off"], g["col"],
+                          g["outdeg"], 20)
+        rel = np.abs(g["pr"].astype(np.float64) - v64) / np.abs(v64)
+        bound = 1e-3 if name.startswith("hub") else 1e-5
+        assert rel.max() < bound, (name, rel.max())
+
+
+def test_weighted_sssp_matches_dijkstra():
+    """Weighted SSSP (uint32 weights, no reference counterpart): the oracle's
+    Jacobi pull fixpoint equals Dijkstra (scipy) on small graphs."""
+    scipy_sparse = pytest.importorskip("scipy.sparse")
+    csgraph = pytest.importorskip("scipy.sparse.csgraph")
+    import graphee_gb300 as gx
+    g = gx.rmat_graph(10, 8, seed=11, P=4, weight_seed=5)
+    vals, _, _ = O.run(O.SSSP, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 1000, weights=g.weights, source=0)
+    dst = np.repeat(np.arange(g.V), np.diff(g.off))
+    A = scipy_sparse.csr_matrix((g.weights.astype(np.float64), (g.col, dst)), shape=(g.V, g.V))
+    d = csgraph.dijkstra(A, directed=True, indices=0)
+    ref = np.where(np.isinf(d), 0xFFFFFFFF, d).astype(np.uint64)
+    assert np.array_equal(vals.astype(np.uint64), ref)
+
+
+def test_cc_matches_scipy_on_symmetric():
+    scipy_sparse = pytest.importorskip("scipy.sparse")
+    csgraph = pytest.importorskip("scipy.sparse.csgraph")
+    import graphee_gb300 as gx
+    g = gx.rmat_graph(11, 4, seed=9, P=8, symmetric=True)
+    vals, _, _ = O.run(O.CC, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 1000)
+    dst = np.repeat(np.arange(g.V), np.diff(g.off))
+    A = scipy_sparse.csr_matrix((np.ones(g.E), (g.col, dst)), shape=(g.V, g.V))
+    n, lab = csgraph.connected_components(A, directed=False)
+    # min vertex id per component
+    mins = np.full(n, g.V)
+    np.minimum.at(mins, lab, np.arange(g.V))
+    assert np.array_equal(vals, mins[lab])
+
+
+def test_pagerank_std_sums_to_one():
+    import graphee_gb300 as gx
+    g = gx.rmat_graph(10, 8, seed=4, P=4)
+    vals, _, _ = O.run(O.PAGERANK_STD, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 200, tolerance=1e-12)
+    assert abs(vals.sum() - 1.0) < 1e-9
+    # fixpoint of r = (1-d)/N + d (A^T D^-1 r + D/N)
+    dst = np.repeat(np.arange(g.V), np.diff(g.off))
+    contrib = np.zeros(g.V)
+    np.add.at(contrib, dst, vals[g.col] / g.outdeg[g.col])
+    D = vals[g.outdeg == 0].sum()
+    fix = 0.15 / g.V + 0.85 * (contrib + D / g.V)
+    assert np.abs(fix - vals).max() < 1e-12
+
+
+def test_triangles_match_networkx():
+    nx = pytest.importorskip("networkx")
+    import graphee_gb300 as gx
+    g = gx.rmat_graph(9, 8, seed=21, P=1, symmetric=True)
+    G = nx.Graph()
+    G.add_nodes_from(range(g.V))
+    dst = np.repeat(np.arange(g.V), np.diff(g.off))
+    G.add_edges_from(zip(g.col.tolist(), dst.tolist()))
+    assert O.triangles(g.V, g.off, g.col) == sum(nx.triangles(G).values()) // 3
