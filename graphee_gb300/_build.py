@@ -23,7 +23,7 @@ if not Path(NVCC).exists():
     NVCC = shutil.which("nvcc") or NVCC
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr",
-                     "-Xcompiler", "-fPIC,-fopenmp,-O3", "-Xptxas", "-v"]
+                     "-Xcompiler", "-fPIC,-fopenmp,-O3", "-Xptxas", "-v"] + os.environ.get("GX_NVCC_FLAGS", "").split()
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-fopenmp", "-Wall", "-Wno-unused-function"]
 
 

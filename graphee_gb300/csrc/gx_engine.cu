@@ -212,7 +212,8 @@ namespace {
 void build_units(gx_engine* e) {
   const int32_t P = e->P;
   const int64_t* off = e->off.data();
-  const int32_t heavy_deg = std::max(e->cfg.heavy_degree, 32);
+  // Exact-order mode never chunks a vertex: each list is folded in order.
+  const int32_t heavy_deg = e->cfg.exact_order ? INT32_MAX : std::max(e->cfg.heavy_degree, 32);
   const int64_t cap = std::max<int64_t>(e->cfg.tile_edges, 32);
   std::vector<std::vector<int2>> su(P);
   std::vector<std::vector<int32_t>> sh(P);
@@ -227,21 +228,20 @@ void build_units(gx_engine* e) {
       cnt = 0;
       edges = 0;
     };
+    // Tiles are runs of up to 32 consecutive vertices; a vertex above the
+    // heavy threshold keeps its lane (masked in the kernel) and also gets
+    // its own chunk units.
     for (int32_t v = s; v < t; ++v) {
       const int64_t d = off[v + 1] - off[v];
-      if (d > heavy_deg) {
-        close(v);
-        sh[p].push_back(v);
-        vb = v + 1;
-        continue;
-      }
-      if (cnt == 32 || (cnt > 0 && edges + d > cap)) {
+      const int64_t light = d > heavy_deg ? 0 : d;
+      if (d > heavy_deg) sh[p].push_back(v);
+      if (cnt == 32 || (cnt > 0 && edges + light > cap)) {
         close(v);
         vb = v;
       }
       if (cnt == 0) vb = v;
       ++cnt;
-      edges += d;
+      edges += light;
     }
     close(t);
   }
@@ -300,12 +300,12 @@ gx_status plan_shards(gx_engine* e) {
     lo[p] = e->off[e->bounds[p]] & ~3ll;
     hi[p] = (e->off[e->bounds[p + 1]] + 3) & ~3ll;
     const int64_t bytes = (hi[p] - lo[p] + 4) * per_edge;
-    if (budget < 0 || used + bytes <= budget) {
+    if (budget < 0 || (used + hi[p] - lo[p] + 4) * per_edge <= budget) {
       e->resident[p] = 1;
-      used += hi[p] - lo[p] + 4;
+      used += hi[p] - lo[p] + 4;  // elements
       ++e->n_resident;
     } else {
-      max_stream = std::max(max_stream, hi[p] - lo[p] + 4);
+      max_stream = std::max(max_stream, bytes / per_edge);
     }
   }
   e->all_resident = e->n_resident == P;
@@ -501,6 +501,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   pa.heavy = e->d_heavy;
   pa.partial = e->d_partial;
   pa.hticket = e->d_hticket;
+  pa.ctr = e->d_work;
+  pa.heavy_deg = e->cfg.exact_order ? INT32_MAX : std::max(e->cfg.heavy_degree, 32);
   pa.bm = e->d_bm;
   PushArgs qa{};
   qa.ctl = e->d_ctl;
@@ -510,7 +512,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   qa.val[0] = e->d_val[0];
   qa.val[1] = e->d_val[1];
   qa.frontier = e->d_frontier;
-  qa.ctr = e->d_work;
+  qa.ctr = e->d_work + kQueues;
   qa.bm = e->d_bm;
   FinArgs fa{};
   fa.ctl = e->d_ctl;
@@ -524,7 +526,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   fa.work_ctr = e->d_work;
   fa.n_work_ctr = e->n_work;
 
-  const int grid_pull = occupancy_grid<APP>(e, reinterpret_cast<const void*>(pull_kernel<APP>));
+  void (*pull)(PullArgs) = e->cfg.exact_order ? pull_kernel<APP, true> : pull_kernel<APP, false>;
+  const int grid_pull = occupancy_grid<APP>(e, reinterpret_cast<const void*>(pull));
   const int grid_push = occupancy_grid<APP>(e, reinterpret_cast<const void*>(push_kernel<APP>));
   const int grid_fin = std::max(1, std::min(e->n_sm * 4, (e->n_words + kThreads - 1) / kThreads));
 
@@ -554,7 +557,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
         });
     auto enqueue = [&](int i) -> gx_status {
       if (prof) GX_CUDA(cudaEventRecord(pev[2 * i], e->s_comp));
-      pull_kernel<APP><<<grid_pull, kThreads, 0, e->s_comp>>>(pa);
+      pull<<<grid_pull, kThreads, 0, e->s_comp>>>(pa);
       if (prof) GX_CUDA(cudaEventRecord(pev[2 * i + 1], e->s_comp));
       if (push_ok) push_kernel<APP><<<grid_push, kThreads, 0, e->s_comp>>>(qa);
       finalize_kernel<APP><<<grid_fin, kThreads, 0, e->s_comp>>>(fa);
@@ -629,6 +632,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
         PullArgs sp = pa;
         sp.u_begin = e->unit_begin[p];
         sp.u_end = e->unit_begin[p + 1];
+        sp.ctr = e->d_work + 2 * kQueues + kQueues * p;
         if (sp.u_end == sp.u_begin) continue;
         const bool active = !sel || ((hc.shard_mask >> (p / e->shard_group)) & 1ull);
         if (e->resident[p] || !active) {
@@ -654,7 +658,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
         }
         const int units = sp.u_end - sp.u_begin;
         const int grid = std::max(1, std::min(grid_pull, (units + kWarps - 1) / kWarps));
-        pull_kernel<APP><<<grid, kThreads, 0, e->s_comp>>>(sp);
+        pull<<<grid, kThreads, 0, e->s_comp>>>(sp);
         GX_CUDA(cudaGetLastError());
         ++launches;
         ++pull_launches;
@@ -731,8 +735,9 @@ void gx_config_default(gx_config* cfg) {
   cfg->cache_budget_bytes = -1;
   cfg->stream_slots = 3;
   cfg->selective_threshold = 0.001;
-  cfg->heavy_degree = 2048;
+  cfg->heavy_degree = 4096;
   cfg->tile_edges = 2048;
+  cfg->exact_order = 0;
   cfg->push_sparse = 1;
   cfg->use_graph = 1;
   cfg->wait_limit = 1u << 22;
@@ -851,7 +856,7 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   e->n_words = (V + 31) / 32 + 2;
   GX_TRY(dev_alloc(&e->d_bm, static_cast<size_t>(e->n_words)));
   GX_TRY(dev_alloc(&e->d_frontier, static_cast<size_t>(V)));
-  e->n_work = 2 * P + 2;
+  e->n_work = kQueues * (P + 2);
   GX_TRY(dev_alloc(&e->d_work, static_cast<size_t>(e->n_work)));
   GX_TRY(plan_shards(e));
   GX_TRY(build_signatures(e));

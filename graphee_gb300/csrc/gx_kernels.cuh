@@ -77,6 +77,8 @@ struct PullArgs {
   const int4* heavy;        // heavy vertex h: (v, n_chunks, partial base, shard)
   void* partial;            // per-chunk partial results (T)
   unsigned int* hticket;    // per heavy vertex: chunks finished this step
+  unsigned int* ctr;        // kQueues work-unit cursors of this launch (reset by finalize)
+  int32_t heavy_deg;        // lists longer than this are swept by their own units
   uint32_t* bm;             // next-frontier bitmap
 };
 
@@ -141,6 +143,12 @@ __device__ __forceinline__ typename AppTraits<APP>::T combine(typename AppTraits
   else return x < acc ? x : acc;
 }
 
+// Per-step scalars the apply step needs.
+struct ApplyCtx {
+  int step;
+  double damping, inv_n, fx_scale, base;
+};
+
 struct LocalAcc {
   unsigned long long changed = 0, active = 0, edges = 0, resid = 0, dangl = 0;
 };
@@ -148,8 +156,8 @@ struct LocalAcc {
 // Apply step for vertex v given its gathered value (end of comp_* + end_comp):
 // writes MsgNew[v] (and the next contribution), counts changes.
 template <int APP>
-__device__ __forceinline__ bool apply_vertex(const PullArgs& a, const Ctl& c, int v, typename AppTraits<APP>::T acc,
-                                             typename AppTraits<APP>::T old, void* dst_val, float* dst_con,
+__device__ __forceinline__ bool apply_vertex(const ApplyCtx c, int v, typename AppTraits<APP>::T acc,
+                                             typename AppTraits<APP>::T old, int32_t od, void* dst_val, float* dst_con,
                                              LocalAcc& la) {
   typedef typename AppTraits<APP>::T T;
   T nv;
@@ -164,7 +172,6 @@ __device__ __forceinline__ bool apply_vertex(const PullArgs& a, const Ctl& c, in
   }
   static_cast<T*>(dst_val)[v] = nv;
   if constexpr (is_pr<APP>()) {
-    const int32_t od = __ldg(a.outdeg + v);
     dst_con[v] = nv / static_cast<float>(od > 0 ? od : 1);  // Msg[u]/_VertexOut[u], clamp pagerank.cpp:77-80
     const double diff = fabs(static_cast<double>(nv) - static_cast<double>(old));
     la.resid += __double2ull_rn(diff * c.fx_scale);
@@ -197,18 +204,36 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long x) {
 }
 
 // ---------------------------------------------------------------------------
-// Pull.  The swept vertices are cut into warp-sized work units with bounded
-// edge counts, assigned to warps round-robin (no global work counter):
-//  * a tile of up to 32 consecutive light vertices stages its contiguous edge
-//    range through shared memory (128-bit streaming index loads, one gather
-//    per edge); each lane then folds its own vertex's edges in ascending edge
-//    order, which is the reference's summation order (pagerank.cpp:44-47);
-//  * a heavy vertex is split into chunks of kHeavyChunk edges; each chunk is
-//    reduced by one warp in a fixed lane pattern, and the warp that finishes
-//    the last chunk folds the per-chunk partials in chunk order and applies
-//    the vertex.  Results are deterministic run to run.
+// Pull.  The swept vertices are cut into warp work units of bounded size,
+// which warps claim a few at a time from a per-launch counter:
+//  * a tile of up to 32 consecutive vertices of in-degree <= heavy: lanes
+//    with in-degree <= kLaneMaxDegree walk their own edge list (two 128-bit
+//    index loads per step, next pair prefetched) and fold in edge order,
+//    which is the reference's summation order (pagerank.cpp:44-47); lanes
+//    with more edges are then swept by the whole warp one by one (coalesced
+//    index loads, a fixed-shape tree sum);
+//  * a heavy vertex (in-degree > heavy) is split into chunks of kHeavyChunk
+//    edges; each chunk is reduced by one warp, and the warp that finishes a
+//    vertex's last chunk folds the partials in chunk order and applies it.
+// In exact-order mode (EXACT) every vertex is folded sequentially in edge
+// order: tiles with a longer list stage their edge range through shared
+// memory and each lane folds its own slice; no vertex is chunked.
+// Results are deterministic run to run in both modes.
 // ---------------------------------------------------------------------------
-constexpr int kHeavyChunk = 4096;
+constexpr int kHeavyChunk = 2048;
+constexpr int kLaneMaxDegree = 32;   // longest list a lane walks alone
+constexpr int kGrab = 4;             // units a warp claims per atomic
+constexpr int kQueues = 64;          // work-unit cursors per launch
+
+template <class T>
+__device__ __forceinline__ void store4(T* dst, const T (&x)[4]) {
+  uint4 u;
+  memcpy(&u.x, &x[0], 4);
+  memcpy(&u.y, &x[1], 4);
+  memcpy(&u.z, &x[2], 4);
+  memcpy(&u.w, &x[3], 4);
+  *reinterpret_cast<uint4*>(dst) = u;
+}
 
 template <int APP>
 __device__ __forceinline__ typename AppTraits<APP>::T identity() {
@@ -241,14 +266,53 @@ __device__ __forceinline__ void flush_block(Ctl* ctl, const LocalAcc& la) {
   }
 }
 
+// Warp-cooperative reduction of the edge range [b, e) (all lanes call it with
+// the same range): lanes take 8 consecutive edges each per round, with
+// 128-bit loads; the per-lane partials are combined by a fixed xor tree.
 template <int APP>
-__global__ void __launch_bounds__(kThreads) pull_kernel(PullArgs a) {
+__device__ __forceinline__ typename AppTraits<APP>::T warp_reduce_range(const PullArgs& a, const void* src_val,
+                                                                        const float* src_con, int64_t b, int64_t e,
+                                                                        int lane) {
   typedef typename AppTraits<APP>::T T;
-  __shared__ T s_buf[kWarps][kChunk];
+  T acc = identity<APP>();
+  for (int64_t q = (b & ~3ll) + 4 * lane; q < e; q += 256) {
+    const int64_t q2 = q + 128;
+    const int4 c4 = __ldcs(reinterpret_cast<const int4*>(a.col + q));
+    int4 d4 = make_int4(0, 0, 0, 0);
+    if (q2 < e) d4 = __ldcs(reinterpret_cast<const int4*>(a.col + q2));
+    uint4 w4 = make_uint4(0, 0, 0, 0), x4 = make_uint4(0, 0, 0, 0);
+    if constexpr (APP == K_SSSP_W) {
+      w4 = __ldcs(reinterpret_cast<const uint4*>(a.w + q));
+      if (q2 < e) x4 = __ldcs(reinterpret_cast<const uint4*>(a.w + q2));
+    }
+    const int cs[8] = {c4.x, c4.y, c4.z, c4.w, d4.x, d4.y, d4.z, d4.w};
+    const uint32_t ws[8] = {w4.x, w4.y, w4.z, w4.w, x4.x, x4.y, x4.z, x4.w};
+    T vals[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int64_t k = (j < 4 ? q : q2) + (j & 3);
+      vals[j] = (k >= b && k < e) ? edge_value<APP>(a, src_val, src_con, cs[j], ws[j]) : identity<APP>();
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc = combine<APP>(acc, vals[j]);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc = combine<APP>(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+  return acc;
+}
+
+#ifndef GX_PULL_MIN_BLOCKS
+#define GX_PULL_MIN_BLOCKS 5
+#endif
+
+template <int APP, bool EXACT>
+__global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(PullArgs a) {
+  typedef typename AppTraits<APP>::T T;
+  __shared__ __align__(16) T s_buf[EXACT ? kWarps : 1][EXACT ? kChunk : 4];
   Ctl* ctl = a.ctl;
   const int done = ctl->done, mode = ctl->mode;
   if (done || mode == MODE_PUSH) return;
-  Ctl c;
+  ApplyCtx c;
   c.step = ctl->step;
   c.damping = ctl->damping;
   c.inv_n = ctl->inv_n;
@@ -257,140 +321,215 @@ __global__ void __launch_bounds__(kThreads) pull_kernel(PullArgs a) {
   const int cur = ctl->cur;
   const int group = ctl->shard_group;
   const unsigned long long smask = ctl->shard_mask;
-  const void* src_val = a.val[cur];
-  void* dst_val = a.val[cur ^ 1];
-  const float* src_con = a.con[cur];
-  float* dst_con = a.con[cur ^ 1];
+  // Ternaries, not a[cur]: indexing a parameter array with a runtime value
+  // would copy the whole parameter block to local memory.
+  const void* src_val = cur ? a.val[1] : a.val[0];
+  void* dst_val = cur ? a.val[0] : a.val[1];
+  const float* src_con = cur ? a.con[1] : a.con[0];
+  float* dst_con = cur ? a.con[0] : a.con[1];
   const bool selective = mode == MODE_SELECTIVE;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int gw = blockIdx.x * kWarps + wid;
-  const int nw = gridDim.x * kWarps;
-  T* buf = s_buf[wid];
+  T* buf = s_buf[EXACT ? wid : 0];
   LocalAcc la;
 
-  for (int u = a.u_begin + gw; u < a.u_end; u += nw) {
-    const int2 wu = a.units[u];
-    const bool on = !selective || ((smask >> (a.unit_shard[u] / group)) & 1ull);
-    if (wu.x < 0) {
-      // ---- heavy chunk ----
-      const int h = -wu.x - 1;
-      const int4 H = a.heavy[h];
-      const int v = H.x;
+  // Units are split into up to kQueues contiguous ranges, each with its own
+  // cursor; a warp starts on queue (warp id mod queues) and moves on to the
+  // next queue when its own is drained, so cursors see little contention.
+  const int U = a.u_end - a.u_begin;
+  const int nq = U / 256 < 1 ? 1 : (U / 256 < kQueues ? U / 256 : kQueues);
+  const int gw = blockIdx.x * kWarps + wid;
+  int q = gw % nq;
+  for (int visited = 0; visited < nq;) {
+    const int qb = a.u_begin + static_cast<int>((static_cast<int64_t>(U) * q) / nq);
+    const int qe = a.u_begin + static_cast<int>((static_cast<int64_t>(U) * (q + 1)) / nq);
+    int u0 = 0;
+    if (lane == 0) u0 = qb + static_cast<int>(atomicAdd(a.ctr + q, static_cast<unsigned>(kGrab)));
+    u0 = __shfl_sync(0xffffffffu, u0, 0);
+    if (u0 >= qe) {
+      q = q + 1 == nq ? 0 : q + 1;
+      ++visited;
+      continue;
+    }
+    const int cnt = qe - u0 < kGrab ? qe - u0 : kGrab;
+    // One coalesced load for the batch's descriptors.
+    int2 myu = make_int2(0, 0);
+    int mysh = 0;
+    if (lane < cnt) {
+      myu = a.units[u0 + lane];
+      if (selective) mysh = a.unit_shard[u0 + lane];
+    }
+    for (int j = 0; j < cnt; ++j) {
+      const int2 wu = make_int2(__shfl_sync(0xffffffffu, myu.x, j), __shfl_sync(0xffffffffu, myu.y, j));
+      const bool on = !selective || ((smask >> (__shfl_sync(0xffffffffu, mysh, j) / group)) & 1ull);
+      if (wu.x < 0) {
+        // ---- heavy chunk ----
+        const int h = -wu.x - 1;
+        const int4 H = a.heavy[h];
+        const int v = H.x;
+        if (!on) {
+          if (wu.y == 0 && lane == 0) {
+            static_cast<T*>(dst_val)[v] = static_cast<const T*>(src_val)[v];
+            if constexpr (is_pr<APP>()) dst_con[v] = src_con[v];
+          }
+          continue;
+        }
+        const int64_t vb = a.off[v], ve = a.off[v + 1];
+        const int64_t b = vb + static_cast<int64_t>(wu.y) * kHeavyChunk;
+        const int64_t e = ve < b + kHeavyChunk ? ve : b + kHeavyChunk;
+        T acc = identity<APP>();
+        if constexpr (APP != K_INDEG) acc = warp_reduce_range<APP>(a, src_val, src_con, b, e, lane);
+        if (lane == 0) {
+          la.edges += e - b;
+          T* part = static_cast<T*>(a.partial);
+          bool last = H.y == 1;
+          if (!last) {
+            part[H.z + wu.y] = acc;
+            __threadfence();
+            last = atomicAdd(a.hticket + h, 1u) == static_cast<unsigned>(H.y) - 1;
+          }
+          if (last) {
+            __threadfence();
+            const volatile T* vp = part;
+            T tot = acc;
+            if (H.y > 1) {
+              tot = identity<APP>();
+              for (int i = 0; i < H.y; ++i) tot = combine<APP>(tot, vp[H.z + i]);
+              a.hticket[h] = 0;
+            }
+            const T old = static_cast<const T*>(src_val)[v];
+            const int32_t od = is_pr<APP>() ? a.outdeg[v] : 0;
+            T fin;
+            if constexpr (is_pr<APP>()) fin = tot;
+            else if constexpr (APP == K_INDEG) fin = static_cast<T>(ve - vb);
+            else fin = combine<APP>(old, tot);
+            if (apply_vertex<APP>(c, v, fin, old, od, dst_val, dst_con, la)) atomicOr(a.bm + (v >> 5), 1u << (v & 31));
+          }
+        }
+        continue;
+      }
+      // ---- tile ----
+      const int vb = wu.x, n = wu.y - wu.x;
+      const int v = vb + lane;
+      int64_t beg = 0, end = 0;
+      T old = T(0);
+      int32_t od = 0;
+      if (lane < n) {
+        beg = a.off[v];
+        end = a.off[v + 1];
+      }
+      // Vertices above the heavy threshold are applied by their own units.
+      const bool valid = lane < n && end - beg <= a.heavy_deg;
+      if (valid) {
+        old = __ldcs(static_cast<const T*>(src_val) + v);
+        if constexpr (is_pr<APP>()) od = __ldcs(a.outdeg + v);
+      }
       if (!on) {
-        if (wu.y == 0 && lane == 0) {
-          static_cast<T*>(dst_val)[v] = static_cast<const T*>(src_val)[v];
+        if (valid) {
+          static_cast<T*>(dst_val)[v] = old;
           if constexpr (is_pr<APP>()) dst_con[v] = src_con[v];
         }
         continue;
       }
-      const int64_t vb = a.off[v], ve = a.off[v + 1];
-      const int64_t b = vb + static_cast<int64_t>(wu.y) * kHeavyChunk;
-      const int64_t e = ve < b + kHeavyChunk ? ve : b + kHeavyChunk;
-      T acc = identity<APP>();
-      if constexpr (APP != K_INDEG) {
-        for (int64_t q = (b & ~3ll) + 4 * lane; q < e; q += 256) {
-          const int64_t q2 = q + 128;
-          const int4 c4 = __ldcs(reinterpret_cast<const int4*>(a.col + q));
-          int4 d4 = make_int4(0, 0, 0, 0);
-          if (q2 < e) d4 = __ldcs(reinterpret_cast<const int4*>(a.col + q2));
-          uint4 w4 = make_uint4(0, 0, 0, 0), x4 = make_uint4(0, 0, 0, 0);
-          if constexpr (APP == K_SSSP_W) {
-            w4 = __ldcs(reinterpret_cast<const uint4*>(a.w + q));
-            if (q2 < e) x4 = __ldcs(reinterpret_cast<const uint4*>(a.w + q2));
+      T acc;
+      if constexpr (is_pr<APP>()) acc = 0.f;
+      else acc = old;
+      if constexpr (APP == K_INDEG) {
+        acc = static_cast<T>(end - beg);
+      } else {
+        const bool longl = valid && end - beg > kLaneMaxDegree;
+        const unsigned mlong = __ballot_sync(0xffffffffu, longl);
+        if (EXACT && mlong) {
+          // Stage the tile's edge range; each lane folds its own slice in order.
+          const int64_t E0 = __shfl_sync(0xffffffffu, beg, 0);
+          const int64_t E1 = __shfl_sync(0xffffffffu, end, n - 1);
+          for (int64_t c0 = E0 & ~3ll; c0 < E1; c0 += kChunk) {
+#pragma unroll
+            for (int j = 0; j < kChunk / 128; ++j) {
+              const int64_t q = c0 + 4 * (lane + 32 * j);
+              if (q < E1) {
+                const int4 c4 = __ldcs(reinterpret_cast<const int4*>(a.col + q));
+                uint4 w4 = make_uint4(0, 0, 0, 0);
+                if constexpr (APP == K_SSSP_W) w4 = __ldcs(reinterpret_cast<const uint4*>(a.w + q));
+                const int cs[4] = {c4.x, c4.y, c4.z, c4.w};
+                const uint32_t ws[4] = {w4.x, w4.y, w4.z, w4.w};
+                T x[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                  const int64_t kk = q + e;
+                  x[e] = (kk >= E0 && kk < E1) ? edge_value<APP>(a, src_val, src_con, cs[e], ws[e]) : identity<APP>();
+                }
+                store4(buf + 4 * (lane + 32 * j), x);
+              }
+            }
+            __syncwarp();
+            const int lo = static_cast<int>((beg > c0 ? beg : c0) - c0);
+            const int hi = static_cast<int>((end < c0 + kChunk ? end : c0 + kChunk) - c0);
+#pragma unroll 4
+            for (int kk = lo; kk < hi; ++kk) acc = combine<APP>(acc, buf[kk]);
+            __syncwarp();
           }
-          const int cs[8] = {c4.x, c4.y, c4.z, c4.w, d4.x, d4.y, d4.z, d4.w};
-          const uint32_t ws[8] = {w4.x, w4.y, w4.z, w4.w, x4.x, x4.y, x4.z, x4.w};
-          T vals[8];
-#pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            const int64_t k = (j < 4 ? q : q2) + (j & 3);
-            vals[j] = (k >= b && k < e) ? edge_value<APP>(a, src_val, src_con, cs[j], ws[j]) : identity<APP>();
-          }
-#pragma unroll
-          for (int j = 0; j < 8; ++j) acc = combine<APP>(acc, vals[j]);
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc = combine<APP>(acc, __shfl_xor_sync(0xffffffffu, acc, o));
-      }
-      if (lane == 0) {
-        la.edges += e - b;
-        T* part = static_cast<T*>(a.partial);
-        part[H.z + wu.y] = acc;
-        __threadfence();
-        const unsigned t = atomicAdd(a.hticket + h, 1u);
-        if (t == static_cast<unsigned>(H.y) - 1) {
-          __threadfence();
-          const volatile T* vp = part;
-          T tot = identity<APP>();
-          for (int i = 0; i < H.y; ++i) tot = combine<APP>(tot, vp[H.z + i]);
-          const T old = static_cast<const T*>(src_val)[v];
-          T fin;
-          if constexpr (is_pr<APP>()) fin = tot;
-          else if constexpr (APP == K_INDEG) fin = static_cast<T>(ve - vb);
-          else fin = combine<APP>(old, tot);
-          if (apply_vertex<APP>(a, c, v, fin, old, dst_val, dst_con, la)) atomicOr(a.bm + (v >> 5), 1u << (v & 31));
-          a.hticket[h] = 0;
-        }
-      }
-      continue;
-    }
-    // ---- tile of light vertices ----
-    const int vb = wu.x, n = wu.y - wu.x;
-    const bool valid = lane < n;
-    const int v = vb + lane;
-    int64_t beg = 0, end = 0;
-    T old = T(0);
-    if (valid) {
-      beg = a.off[v];
-      end = a.off[v + 1];
-      old = __ldcs(static_cast<const T*>(src_val) + v);
-    }
-    if (!on) {
-      if (valid) {
-        static_cast<T*>(dst_val)[v] = old;
-        if constexpr (is_pr<APP>()) dst_con[v] = src_con[v];
-      }
-      continue;
-    }
-    const int64_t E0 = __shfl_sync(0xffffffffu, beg, 0);
-    const int64_t E1 = __shfl_sync(0xffffffffu, end, n - 1);
-    T acc;
-    if constexpr (is_pr<APP>()) acc = 0.f;
-    else acc = old;
-    if constexpr (APP != K_INDEG) {
-      for (int64_t c0 = E0 & ~3ll; c0 < E1; c0 += kChunk) {
-#pragma unroll
-        for (int j = 0; j < kChunk / 128; ++j) {
-          const int64_t q = c0 + 4 * (lane + 32 * j);
-          if (q < E1) {
-            const int4 c4 = __ldcs(reinterpret_cast<const int4*>(a.col + q));
-            uint4 w4 = make_uint4(0, 0, 0, 0);
-            if constexpr (APP == K_SSSP_W) w4 = __ldcs(reinterpret_cast<const uint4*>(a.w + q));
-            const int cs[4] = {c4.x, c4.y, c4.z, c4.w};
-            const uint32_t ws[4] = {w4.x, w4.y, w4.z, w4.w};
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              const int64_t k = q + e;
-              if (k >= E0 && k < E1) buf[4 * (lane + 32 * j) + e] = edge_value<APP>(a, src_val, src_con, cs[e], ws[e]);
+        } else {
+          // Short lists: lane per vertex, 8 edges per step, next step prefetched.
+          const int64_t lend = longl ? beg : end;
+          int64_t k = beg & ~3ll;
+          const int steps = (valid && lend > beg) ? static_cast<int>((lend - k + 7) >> 3) : 0;
+          const int smax = static_cast<int>(__reduce_max_sync(0xffffffffu, static_cast<unsigned>(steps)));
+          int4 c0v = make_int4(0, 0, 0, 0), c1v = make_int4(0, 0, 0, 0);
+          uint4 w0v = make_uint4(0, 0, 0, 0), w1v = make_uint4(0, 0, 0, 0);
+          if (steps > 0) {
+            c0v = __ldcs(reinterpret_cast<const int4*>(a.col + k));
+            if (k + 4 < lend) c1v = __ldcs(reinterpret_cast<const int4*>(a.col + k + 4));
+            if constexpr (APP == K_SSSP_W) {
+              w0v = __ldcs(reinterpret_cast<const uint4*>(a.w + k));
+              if (k + 4 < lend) w1v = __ldcs(reinterpret_cast<const uint4*>(a.w + k + 4));
             }
           }
+          for (int st = 0; st < smax; ++st) {
+            if (st < steps) {
+              const int cs[8] = {c0v.x, c0v.y, c0v.z, c0v.w, c1v.x, c1v.y, c1v.z, c1v.w};
+              const uint32_t ws[8] = {w0v.x, w0v.y, w0v.z, w0v.w, w1v.x, w1v.y, w1v.z, w1v.w};
+              const int64_t kn = k + 8;
+              if (kn < lend) {
+                c0v = __ldcs(reinterpret_cast<const int4*>(a.col + kn));
+                if (kn + 4 < lend) c1v = __ldcs(reinterpret_cast<const int4*>(a.col + kn + 4));
+                if constexpr (APP == K_SSSP_W) {
+                  w0v = __ldcs(reinterpret_cast<const uint4*>(a.w + kn));
+                  if (kn + 4 < lend) w1v = __ldcs(reinterpret_cast<const uint4*>(a.w + kn + 4));
+                }
+              }
+              T vals[8];
+#pragma unroll
+              for (int j = 0; j < 8; ++j) {
+                const int64_t kk = k + j;
+                vals[j] = (kk >= beg && kk < lend) ? edge_value<APP>(a, src_val, src_con, cs[j], ws[j])
+                                                   : identity<APP>();
+              }
+#pragma unroll
+              for (int j = 0; j < 8; ++j) {
+                const int64_t kk = k + j;
+                if (kk >= beg && kk < lend) acc = combine<APP>(acc, vals[j]);
+              }
+              k = kn;
+            }
+          }
+          // Longer lists: the whole warp sweeps each one in turn.
+          for (unsigned m = mlong; m; m &= m - 1) {
+            const int l = __ffs(m) - 1;
+            const int64_t bl = __shfl_sync(0xffffffffu, beg, l);
+            const int64_t el = __shfl_sync(0xffffffffu, end, l);
+            const T r = warp_reduce_range<APP>(a, src_val, src_con, bl, el, lane);
+            if (lane == l) acc = combine<APP>(acc, r);
+          }
         }
-        __syncwarp();
-        const int64_t lo = beg > c0 ? beg : c0;
-        const int64_t hi = end < c0 + kChunk ? end : c0 + kChunk;
-        for (int64_t k = lo; k < hi; ++k) acc = combine<APP>(acc, buf[k - c0]);
-        __syncwarp();
       }
-    } else {
-      acc = static_cast<T>(end - beg);
+      bool act = false;
+      if (valid) {
+        la.edges += end - beg;
+        act = apply_vertex<APP>(c, v, acc, old, od, dst_val, dst_con, la);
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, act);
+      if (lane == 0) bitmap_set_tile(a.bm, vb, m);
     }
-    bool act = false;
-    if (valid) {
-      la.edges += end - beg;
-      act = apply_vertex<APP>(a, c, v, acc, old, dst_val, dst_con, la);
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, act);
-    if (lane == 0) bitmap_set_tile(a.bm, vb, m);
   }
   flush_block(ctl, la);
 }
@@ -410,7 +549,7 @@ __global__ void __launch_bounds__(kThreads) push_kernel(PushArgs a) {
   const int nf = a.ctl->n_frontier;
   LocalAcc la;
   if constexpr (!is_pr<APP>() && APP != K_INDEG) {
-  T* val = static_cast<T*>(a.val[cur]);
+  T* val = static_cast<T*>(cur ? a.val[1] : a.val[0]);
   for (;;) {
     int base = 0;
     if (lane == 0) base = static_cast<int>(atomicAdd(a.ctr, 32u));
@@ -467,7 +606,8 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
   const bool sel_next = static_cast<double>(ratio) < c.sel_threshold;
   const bool push_next = sel_next && c.push_ok;
   const bool want_mask = sel_next && !push_next && a.sig != nullptr;
-  const T* newv = static_cast<const T*>(a.val[c.mode == MODE_PUSH ? c.cur : (c.cur ^ 1)]);
+  const int nb = c.mode == MODE_PUSH ? c.cur : (c.cur ^ 1);
+  const T* newv = static_cast<const T*>(nb ? a.val[1] : a.val[0]);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   unsigned long long act = 0, mask = 0;
   for (int w = blockIdx.x * kThreads + threadIdx.x; w < a.n_words; w += gridDim.x * kThreads) {

@@ -1,0 +1,53 @@
+"""Runs one workload of the engine and nothing else, so a profiler sees only
+its kernels:  python -m graphee_gb300.prof --app pagerank --scale 22 --iters 3
+
+Graph: seeded R-MAT (a,b,c=.57,.19,.19), edge factor 16, 256 shards, the
+same generator and seed as bench.py.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import graphee_gb300 as gx
+
+APPS = {"pagerank": gx.APP_PAGERANK_REF, "pagerank_std": gx.APP_PAGERANK_STD, "sssp": gx.APP_SSSP, "cc": gx.APP_CC}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--app", default="pagerank", choices=sorted(APPS))
+    ap.add_argument("--scale", type=int, default=22)
+    ap.add_argument("--edge-factor", type=int, default=16)
+    ap.add_argument("--iters", type=int, default=3)
+    ap.add_argument("--runs", type=int, default=1)
+    ap.add_argument("--graph", type=int, default=0, help="replay supersteps as a CUDA graph")
+    ap.add_argument("--heavy-degree", type=int, default=None)
+    ap.add_argument("--tile-edges", type=int, default=None)
+    ap.add_argument("--profile-kernels", type=int, default=0, help="time each pull launch with CUDA events")
+    a = ap.parse_args()
+    sym = a.app == "cc"
+    g = gx.rmat_graph(a.scale, a.edge_factor, seed=20240601, P=256, symmetric=sym,
+                      weight_seed=7 if a.app == "sssp" else None)
+    cfg = {"use_graph": a.graph, "profile": a.profile_kernels}
+    if a.heavy_degree is not None:
+        cfg["heavy_degree"] = a.heavy_degree
+    if a.tile_edges is not None:
+        cfg["tile_edges"] = a.tile_edges
+    with gx.Engine(**cfg) as e:
+        e.load(g)
+        kw = {"source": 0, "weighted": True} if a.app == "sssp" else {}
+        for _ in range(a.runs):
+            t0 = time.perf_counter()
+            st = e.run(APPS[a.app], a.iters, **kw)
+            st["wall_s"] = time.perf_counter() - t0
+        st.update({"V": g.V, "E": g.E})
+        if st["pull_launches"] and st["ms_pull"]:
+            st["pull_ms_avg"] = st["ms_pull"] / st["pull_launches"]
+            st["pull_alg_GBps"] = (8 * g.E + 24 * g.V) / (st["pull_ms_avg"] / 1e3) / 1e9
+        print(json.dumps(st))
+
+
+if __name__ == "__main__":
+    main()

@@ -64,8 +64,12 @@ typedef struct gx_config {
                                   Replaces EDGE_CACHE_SIZE (GraphMP/system/Global.h:52). */
   int32_t stream_slots;        /* device slots in the streaming ring (>=2, default 3) */
   double selective_threshold;  /* BF_THRE (GraphMP/system/Global.h:57), default 0.001 */
-  int32_t heavy_degree;        /* in-degree above which a vertex gets a whole CTA (default 2048) */
+  int32_t heavy_degree;        /* in-degree above which a vertex gets its own warp units, split
+                                  into 2048-edge chunks (default 4096, minimum 32) */
   int32_t tile_edges;          /* edge cap of one warp tile (default 2048) */
+  int32_t exact_order;         /* 1: fold every vertex's in-edges in edge order, as the reference's
+                                  sequential loop does (PageRank bit-exact); 0: tree sums for
+                                  vertices above heavy_degree (default 0) */
   int32_t push_sparse;         /* SSSP/CC: push over out-edges when selective (default 1) */
   int32_t use_graph;           /* replay the iteration loop as a CUDA graph (default 1) */
   uint32_t wait_limit;         /* iteration cap of every device spin-wait (default 1<<22) */
