@@ -103,6 +103,7 @@ def lib() -> C.CDLL:
         "gx_write_shards": (C.c_int, [C.c_char_p, I32, I32, P, P, P, P]),
         "gx_read_shards": (C.c_int, [C.c_char_p, I32, I32, P, P, P, P, P]),
         "gx_edge_weights": (C.c_int, [U64, I32, P, P, P]),
+        "gx_pagerank_noalloc": (C.c_int, [P, P, I64, I64, P, I32, I32, D, P, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)

@@ -710,7 +710,7 @@ __global__ void init_kernel(Ctl* ctl, void* val, float* con, const int32_t* outd
 
 // Per-vertex shard-group masks: bit g of sig[u] is set iff u is a source in
 // a shard of group g.  Replaces the bloom-filter build (GraphPS.h:225-245).
-__global__ void signature_kernel(unsigned long long* sig, const int32_t* col, int64_t e0, int64_t e1,
+static __global__ void signature_kernel(unsigned long long* sig, const int32_t* col, int64_t e0, int64_t e1,
                                  unsigned long long bit) {
   for (int64_t k = e0 + blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < e1;
        k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -721,7 +721,7 @@ __global__ void signature_kernel(unsigned long long* sig, const int32_t* col, in
 
 // Out-edge CSR from the CSC (counting sort by source; order within a source
 // is unspecified, which min-plus / min-label do not observe).
-__global__ void transpose_kernel(const int64_t* off, const int32_t* col, const uint32_t* w, int n,
+static __global__ void transpose_kernel(const int64_t* off, const int32_t* col, const uint32_t* w, int n,
                                  unsigned long long* cursor, int32_t* ocol, uint32_t* ow) {
   const int lane = threadIdx.x & 31;
   const int warps = gridDim.x * (blockDim.x >> 5);

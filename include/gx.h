@@ -155,6 +155,31 @@ gx_status gx_get_values(gx_engine* e, void* host_out);
  * iteration, GraphPS.h:375-382). */
 gx_status gx_get_iter_stats(gx_engine* e, int32_t step, gx_iter_stats* out);
 
+/* PageRank with the reference's semantics (GX_APP_PAGERANK_REF, default
+ * tree-sum mode) over a CSC the caller already holds in device memory, for
+ * callers that cannot allocate device memory themselves or let a library do
+ * it: a plugin inside a host application whose allocator owns the GPU, a
+ * serving path that must not allocate per request, or a process that has
+ * reserved the device for its own pool.  No counterpart in the reference.
+ *
+ * Allocates nothing: its scratch is a fixed 12.7 MB array in the library's
+ * device image, present on every GPU that loads the library until exit,
+ * which bounds V to 1,048,576 and max_iter to 1024 (larger sizes are
+ * rejected with GX_ERR_INVALID).  d_off int64[V+1], d_col int32 with room for
+ * num_edges + 4 entries (col_capacity; the last four are read but unused),
+ * d_outdeg int32[V]; d_rank float[V] receives the ranks.  All device
+ * pointers; `stream` is a cudaStream_t (NULL = legacy default stream).
+ * The first call on each device looks up the scratch's device address with
+ * that device current; make that first call before any stream capture.
+ * Every call reuses the same scratch and resets it first, so calls that may
+ * overlap on the GPU (other streams, other host threads) race with each
+ * other and must be serialised by the caller.  iterations_out (nullable)
+ * synchronises the stream and returns the supersteps run. */
+gx_status gx_pagerank_noalloc(const int64_t* d_off, const int32_t* d_col, int64_t num_edges,
+                              int64_t col_capacity, const int32_t* d_outdeg, int32_t V,
+                              int32_t max_iter, double damping, float* d_rank, void* stream,
+                              int32_t* iterations_out);
+
 /* ---- graph construction and the reference's on-disk format (host) ---- */
 
 enum { GX_BUILD_DROP_SELF = 1, GX_BUILD_DEDUP = 2, GX_BUILD_SYMMETRIZE = 4 };
