@@ -62,6 +62,13 @@ class RunStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class BatchTuning(C.Structure):
+    _fields_ = [("threads", C.c_int32), ("lane_max", C.c_int32), ("ctas_per_sm", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class IterStats(C.Structure):
     _fields_ = [("changed", C.c_int64), ("active", C.c_int64), ("shards_active", C.c_int32),
                 ("mode", C.c_int32), ("residual_l1", C.c_double), ("dangling", C.c_double),
@@ -104,6 +111,11 @@ def lib() -> C.CDLL:
         "gx_read_shards": (C.c_int, [C.c_char_p, I32, I32, P, P, P, P, P]),
         "gx_edge_weights": (C.c_int, [U64, I32, P, P, P]),
         "gx_pagerank_noalloc": (C.c_int, [P, P, I64, I64, P, I32, I32, D, P, P, P]),
+        "gx_triangle_count": (C.c_int, [P, P, P]),
+        "gx_ppr": (C.c_int, [P, I32, P, I32, D, P, P]),
+        "gx_batch_tuning_default": (None, [P]),
+        "gx_batch_run": (C.c_int, [P, I32, P, I32, I32, D, P, P, P, P, P, P]),
+        "gx_batch_autotune": (C.c_int, [P, I32, P, I32, I32, C.c_char_p, P, P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -230,6 +242,27 @@ def read_shards(directory: str, V: int, P: int) -> Graph:
     return Graph(V, off, col[:E.value].copy(), od, P, bounds)
 
 
+def batch_graph(n: int, scales=(10, 17), edge_factors=(8, 32), seed: int = 1, a=0.57, b=0.19, c=0.19):
+    """n independent seeded R-MAT graphs (scale and edge factor drawn
+    uniformly from the inclusive ranges, per-graph seeds), packed side by
+    side into one Graph.  Returns (graph, inst_vbegin int32[n+1])."""
+    rng = np.random.default_rng(seed)
+    sc = rng.integers(scales[0], scales[1] + 1, size=n)
+    ef = rng.integers(edge_factors[0], edge_factors[1] + 1, size=n)
+    offs, cols, vbeg, ebase = [], [], [0], 0
+    for i in range(n):
+        V = 1 << int(sc[i])
+        src, dst = rmat_edges(int(sc[i]), int(ef[i]) * V, seed * 1000003 + i, a, b, c)
+        off, col = build_csc(V, src, dst)
+        offs.append(off[:-1] + ebase)
+        cols.append(col + vbeg[-1])
+        ebase += int(off[-1])
+        vbeg.append(vbeg[-1] + V)
+    off = np.concatenate(offs + [np.array([ebase], np.int64)])
+    col = np.concatenate(cols) if cols else np.zeros(0, np.int32)
+    return Graph(vbeg[-1], off, col, None, 1), np.array(vbeg, np.int32)
+
+
 # ---------------------------------------------------------------- engine ----
 
 def default_config(**kw) -> Config:
@@ -318,6 +351,52 @@ class Engine:
         if self.app == APP_SSSP and self._weighted:
             return out
         return out.view(np.int32)
+
+    def triangle_count(self) -> tuple[int, dict]:
+        """Exact triangle count of the loaded (symmetric) graph."""
+        tot = C.c_uint64(0)
+        st = RunStats()
+        _check(lib().gx_triangle_count(self._h, C.byref(tot), C.byref(st)), "gx_triangle_count")
+        return int(tot.value), st.as_dict()
+
+    def ppr(self, sources, iters: int, restart: float = 0.15, fetch: bool = True):
+        """Personalized PageRank for len(sources) <= 64 columns; returns
+        (R float32[V, k] or None, stats)."""
+        src = np.ascontiguousarray(sources, np.int32)
+        out = np.empty((self.V, len(src)), np.float32) if fetch else None
+        st = RunStats()
+        _check(lib().gx_ppr(self._h, len(src), _ptr(src), iters, restart, _ptr(out), C.byref(st)), "gx_ppr")
+        return out, st.as_dict()
+
+    def batch_run(self, inst_vbegin, pr_iters=30, cc_max_iter=1000, damping=0.85, tuning: dict | None = None):
+        """Batched PageRank + CC over the packed instances (one persistent
+        launch).  Returns (pr float32[V], cc int32[V], pr_steps, cc_steps, stats)."""
+        vb = np.ascontiguousarray(inst_vbegin, np.int32)
+        n = len(vb) - 1
+        t = None
+        if tuning is not None:
+            t = BatchTuning()
+            lib().gx_batch_tuning_default(C.byref(t))
+            for k, v in tuning.items():
+                setattr(t, k, v)
+        pr = np.empty(self.V, np.float32)
+        cc = np.empty(self.V, np.int32)
+        ps = np.empty(n, np.int32)
+        cs = np.empty(n, np.int32)
+        st = RunStats()
+        _check(lib().gx_batch_run(self._h, n, _ptr(vb), pr_iters, cc_max_iter, damping,
+                                  None if t is None else C.byref(t), _ptr(pr), _ptr(cc), _ptr(ps), _ptr(cs),
+                                  C.byref(st)), "gx_batch_run")
+        return pr, cc, ps, cs, st.as_dict()
+
+    def batch_autotune(self, inst_vbegin, pr_iters=30, cc_max_iter=1000, table_path: str | None = None):
+        vb = np.ascontiguousarray(inst_vbegin, np.int32)
+        best = BatchTuning()
+        ms = C.c_double(0)
+        _check(lib().gx_batch_autotune(self._h, len(vb) - 1, _ptr(vb), pr_iters, cc_max_iter,
+                                       None if table_path is None else str(table_path).encode(), C.byref(best),
+                                       C.byref(ms)), "gx_batch_autotune")
+        return best.as_dict(), ms.value
 
     def iter_stats(self, step: int) -> dict:
         s = IterStats()

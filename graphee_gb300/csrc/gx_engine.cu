@@ -25,185 +25,9 @@
 #include <string>
 #include <vector>
 
-#include "gx_internal.h"
-#include "gx_kernels.cuh"
+#include "gx_engine.h"
 
 using namespace gx;
-
-#define GX_CUDA(call)                                                                                   \
-  do {                                                                                                  \
-    cudaError_t err_ = (call);                                                                          \
-    if (err_ != cudaSuccess)                                                                            \
-      return fail(err_ == cudaErrorMemoryAllocation ? GX_ERR_OOM : GX_ERR_CUDA, "%s:%d %s: %s", __FILE__, \
-                  __LINE__, #call, cudaGetErrorString(err_));                                          \
-  } while (0)
-
-#define GX_TRY(call)                 \
-  do {                               \
-    gx_status st_ = (call);          \
-    if (st_ != GX_OK) return st_;    \
-  } while (0)
-
-namespace {
-
-template <class T>
-gx_status dev_alloc(T** p, size_t n) {
-  if (*p) {
-    cudaFree(*p);
-    *p = nullptr;
-  }
-  if (n == 0) n = 1;
-  cudaError_t err = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
-  if (err != cudaSuccess) {
-    *p = nullptr;
-    cudaGetLastError();
-    return fail(GX_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(err));
-  }
-  return GX_OK;
-}
-
-template <class T>
-void dev_free(T** p) {
-  if (*p) cudaFree(*p);
-  *p = nullptr;
-}
-
-int app_kind(const gx_run_params& p) {
-  switch (p.app) {
-    case GX_APP_PAGERANK_REF: return K_PR_REF;
-    case GX_APP_PAGERANK_STD: return K_PR_STD;
-    case GX_APP_SSSP: return p.weighted ? K_SSSP_W : K_SSSP_UNIT;
-    case GX_APP_CC: return K_CC;
-    case GX_APP_INDEGREE: return K_INDEG;
-  }
-  return -1;
-}
-
-}  // namespace
-
-struct gx_engine {
-  gx_config cfg{};
-  int dev = 0;
-  int n_sm = 0;
-  cudaStream_t s_comp = nullptr, s_copy = nullptr;
-  bool loaded = false;
-
-  // graph (host side)
-  int32_t V = 0, P = 0;
-  int64_t E = 0;
-  std::vector<int32_t> bounds;
-  std::vector<int64_t> off;
-  std::vector<int32_t> outdeg;
-  std::vector<int2> units;
-  std::vector<int32_t> unit_shard;
-  std::vector<int32_t> unit_begin;  // P+1
-  std::vector<int4> heavy;
-  int64_t n_partials = 0;
-
-  // shard cache
-  std::vector<char> resident;
-  std::vector<int64_t> dev_base;    // element offset of a resident shard's slice in d_col
-  int32_t n_resident = 0;
-  bool all_resident = true;
-  int32_t* h_col = nullptr;         // pinned full copy when some shards stream
-  uint32_t* h_w = nullptr;
-  int64_t slot_elems = 0;
-  std::vector<int32_t*> slot_col;
-  std::vector<uint32_t*> slot_w;
-  std::vector<cudaEvent_t> slot_free, slot_ready;
-
-  // device
-  int64_t* d_off = nullptr;
-  int32_t* d_col = nullptr;
-  uint32_t* d_w = nullptr;
-  bool has_weights = false;
-  std::vector<uint32_t> w_host;     // kept until the shard plan is fixed
-  int32_t* d_outdeg = nullptr;
-  void* d_val[2] = {nullptr, nullptr};
-  float* d_con[2] = {nullptr, nullptr};
-  int2* d_units = nullptr;
-  int32_t* d_unit_shard = nullptr;
-  int4* d_heavy = nullptr;
-  void* d_partial = nullptr;
-  unsigned int* d_hticket = nullptr;
-  uint32_t* d_bm = nullptr;
-  int32_t n_words = 0;
-  unsigned long long* d_sig = nullptr;
-  int2* d_frontier = nullptr;
-  int64_t* d_ooff = nullptr;
-  int32_t* d_ocol = nullptr;
-  uint32_t* d_ow = nullptr;
-  bool out_built = false, out_weighted = false;
-  Ctl* d_ctl = nullptr;
-  Ctl* h_ctl = nullptr;
-  StepStats* d_stats = nullptr;
-  int32_t stats_cap = 0;
-  unsigned int* d_work = nullptr;
-  int32_t n_work = 0;
-  int32_t shard_group = 1;
-
-  std::vector<uint32_t> init_vals;
-  bool has_init = false;
-
-  // last run
-  gx_app last_app = GX_APP_PAGERANK_REF;
-  int32_t last_steps = 0;
-  std::vector<StepStats> last_stats;
-  gx_run_stats last_run{};
-
-  ~gx_engine() { release(); }
-
-  void release_graph() {
-    dev_free(&d_off);
-    dev_free(&d_col);
-    dev_free(&d_w);
-    dev_free(&d_outdeg);
-    for (int i = 0; i < 2; ++i) {
-      dev_free(&d_val[i]);
-      dev_free(&d_con[i]);
-    }
-    dev_free(&d_units);
-    dev_free(&d_unit_shard);
-    dev_free(&d_heavy);
-    dev_free(&d_partial);
-    dev_free(&d_hticket);
-    dev_free(&d_bm);
-    dev_free(&d_sig);
-    dev_free(&d_frontier);
-    dev_free(&d_ooff);
-    dev_free(&d_ocol);
-    dev_free(&d_ow);
-    dev_free(&d_stats);
-    dev_free(&d_work);
-    for (auto p : slot_col) cudaFree(p);
-    for (auto p : slot_w) cudaFree(p);
-    slot_col.clear();
-    slot_w.clear();
-    for (auto ev : slot_free) cudaEventDestroy(ev);
-    for (auto ev : slot_ready) cudaEventDestroy(ev);
-    slot_free.clear();
-    slot_ready.clear();
-    if (h_col) cudaFreeHost(h_col);
-    if (h_w) cudaFreeHost(h_w);
-    h_col = nullptr;
-    h_w = nullptr;
-    out_built = false;
-    has_weights = false;
-    loaded = false;
-    stats_cap = 0;
-  }
-
-  void release() {
-    cudaSetDevice(dev);
-    release_graph();
-    dev_free(&d_ctl);
-    if (h_ctl) cudaFreeHost(h_ctl);
-    h_ctl = nullptr;
-    if (s_comp) cudaStreamDestroy(s_comp);
-    if (s_copy) cudaStreamDestroy(s_copy);
-    s_comp = s_copy = nullptr;
-  }
-};
 
 namespace {
 

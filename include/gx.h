@@ -155,6 +155,52 @@ gx_status gx_get_values(gx_engine* e, void* host_out);
  * iteration, GraphPS.h:375-382). */
 gx_status gx_get_iter_stats(gx_engine* e, int32_t step, gx_iter_stats* out);
 
+/* Triangles of the loaded graph taken as undirected (load the CSC of a
+ * symmetrised, deduplicated edge list).  Orients u->v iff (deg u, u) <
+ * (deg v, v) and intersects sorted out-lists.  No reference counterpart:
+ * GraphH/list/system/GraphPS.h:15-95 ("tc") counts reciprocal edges, not
+ * triangles.  *total receives the exact count. */
+gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_stats* stats);
+
+/* Personalized PageRank for k <= 64 sources at once, as one sparse x dense
+ * product per step over the loaded CSC: R <- restart*S + (1-restart)*A^T
+ * D^-1 R, R0 = S (one-hot columns), dangling mass dropped, FP32.  No
+ * reference counterpart (PageRank's pull, pagerank.cpp:44-48, on k vectors).
+ * host_out (nullable) receives R as float[V][k], row-major. */
+gx_status gx_ppr(gx_engine* e, int32_t k, const int32_t* sources, int32_t iters, double restart,
+                 float* host_out, gx_run_stats* stats);
+
+/* Launch schedule of the batched kernel (chosen by gx_batch_autotune). */
+typedef struct gx_batch_tuning {
+  int32_t threads;      /* threads per CTA (multiple of 32, 64..1024) */
+  int32_t lane_max;     /* in-lists up to this length are walked by one lane */
+  int32_t ctas_per_sm;  /* resident CTAs per SM requested */
+} gx_batch_tuning;
+
+void gx_batch_tuning_default(gx_batch_tuning* t);
+
+/* Many independent graphs packed into the loaded CSC (instance i owns
+ * vertices [inst_vbegin[i], inst_vbegin[i+1]) and only edges among them),
+ * run in ONE persistent launch replayed as a CUDA graph: for each instance
+ * the reference's PageRank (pagerank.cpp, N = instance size) for up to
+ * pr_iters supersteps, then its min-label CC (cc.cpp) until no label
+ * changes (at most cc_max_iter), each with GraphPS::run's stop rule
+ * (GraphPS.h:383) per instance.  pr_out float[V], cc_out int32[V]
+ * (instance-local labels), pr_steps / cc_steps int32[n_inst]; all
+ * nullable.  No reference counterpart for the batching itself. */
+gx_status gx_batch_run(gx_engine* e, int32_t n_inst, const int32_t* inst_vbegin, int32_t pr_iters,
+                       int32_t cc_max_iter, double damping, const gx_batch_tuning* tuning,
+                       float* pr_out, int32_t* cc_out, int32_t* pr_steps, int32_t* cc_steps,
+                       gx_run_stats* stats);
+
+/* Times the batched launch under candidate schedules (threads per CTA,
+ * lane_max, CTAs per SM) on the loaded batch, returns the fastest, and
+ * appends a JSON line with every candidate's time to table_path
+ * (nullable). */
+gx_status gx_batch_autotune(gx_engine* e, int32_t n_inst, const int32_t* inst_vbegin, int32_t pr_iters,
+                            int32_t cc_max_iter, const char* table_path, gx_batch_tuning* best,
+                            double* best_ms);
+
 /* PageRank with the reference's semantics (GX_APP_PAGERANK_REF, default
  * tree-sum mode) over a CSC the caller already holds in device memory, for
  * callers that cannot allocate device memory themselves or let a library do

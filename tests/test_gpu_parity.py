@@ -189,3 +189,92 @@ def test_set_init_and_errors():
     e.run(gx.APP_PAGERANK_REF, 7, use_init=True)
     ref, _, _ = O.run(O.PAGERANK_REF, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 7, init=init)
     assert np.abs(e.values() - ref).max() / ref.max() < 1e-5
+
+
+def test_triangle_count_vs_oracle(golden_cases):
+    for seed, scale in [(21, 12), (8, 15)]:
+        g = gx.rmat_graph(scale, 16, seed=seed, P=4, symmetric=True)
+        with engine_for(g) as e:
+            t, st = e.triangle_count()
+        assert t == O.triangles(g.V, g.off, g.col)
+        assert st["edges_scanned"] > 0
+    c = golden_cases["rmat12_sym_p8"]
+    with engine_for(golden_graph(c)) as e:
+        assert e.triangle_count()[0] == O.triangles(int(c["V"]), c["off"], c["col"])
+
+
+def test_triangle_count_clique_uses_cta_path():
+    """K_1200: every orientation list of the first vertices exceeds a warp's
+    shared-memory slice, so the CTA path runs; C(1200, 3) triangles, plus a
+    disjoint 4-cycle with a chord (2 triangles) and isolated vertices."""
+    n = 1200
+    iu = np.triu_indices(n, 1)
+    src = np.concatenate([iu[0], [n, n + 1, n + 2, n + 3, n]])
+    dst = np.concatenate([iu[1], [n + 1, n + 2, n + 3, n, n + 2]])
+    V = n + 10
+    off, col = gx.build_csc(V, src.astype(np.int32), dst.astype(np.int32),
+                            gx.BUILD_DROP_SELF | gx.BUILD_DEDUP | gx.BUILD_SYMMETRIZE)
+    g = gx.Graph(V, off, col, None, 3)
+    with engine_for(g) as e:
+        t, _ = e.triangle_count()
+    assert t == n * (n - 1) * (n - 2) // 6 + 2
+
+
+def test_triangle_count_empty_graph():
+    g = gx.Graph(16, np.zeros(17, np.int64), np.zeros(0, np.int32), None, 2)
+    with engine_for(g) as e:
+        assert e.triangle_count()[0] == 0
+
+
+@pytest.mark.parametrize("k", [64, 5])
+def test_ppr_vs_fp64(k):
+    g = gx.rmat_graph(13, 16, seed=17, P=4)
+    rng = np.random.default_rng(k)
+    src = rng.integers(0, g.V, size=k).astype(np.int32)
+    src[0] = int(np.argmax(np.diff(g.off)))       # a hub source (chunked rows)
+    ref = O.ppr(g.V, g.off, g.col, g.outdeg, src, 15, 0.15)
+    with engine_for(g) as e:
+        R, st = e.ppr(src, 15)
+        R2, _ = e.ppr(src, 15)
+    assert np.array_equal(R, R2)                   # deterministic
+    assert np.abs(R - ref).max() < 1e-6
+    assert np.all(np.abs(R - ref).sum(axis=0) < 1e-5 * np.maximum(1.0, ref.sum(axis=0)))
+    assert st["iterations"] == 15
+
+
+def _instance(g, vb, i):
+    b, e = int(vb[i]), int(vb[i + 1])
+    off = g.off[b:e + 1] - g.off[b]
+    col = g.col[g.off[b]:g.off[e]] - b
+    return e - b, off, col, g.outdeg[b:e]
+
+
+def test_batched_pagerank_cc_vs_oracle(tmp_path):
+    g, vb = gx.batch_graph(40, scales=(5, 11), edge_factors=(2, 16), seed=3)
+    with engine_for(g) as e:
+        pr, cc, ps, cs, st = e.batch_run(vb, pr_iters=30, cc_max_iter=1000)
+        best, ms = e.batch_autotune(vb, pr_iters=30, cc_max_iter=1000, table_path=tmp_path / "tune.jsonl")
+        pr2, cc2, _, _, _ = e.batch_run(vb, pr_iters=30, cc_max_iter=1000, tuning=best)
+    assert st["kernel_launches"] == 1 and ms > 0
+    assert (tmp_path / "tune.jsonl").read_text().count("candidates") == 1
+    for i in range(len(vb) - 1):
+        n, off, col, od = _instance(g, vb, i)
+        b = np.array([0, n], np.int32)
+        ref, ch, _ = O.run(O.PAGERANK_REF, n, 1, b, off, col, od, 30)
+        sl = slice(vb[i], vb[i + 1])
+        assert np.abs(pr[sl] - ref).max() / ref.max() < 1e-5, i
+        assert ps[i] == len(ch)
+        lab, chc, _ = O.run(O.CC, n, 1, b, off, col, od, 1000)
+        assert np.array_equal(cc[sl], lab), i
+        assert cs[i] == len(chc)
+    assert np.array_equal(cc, cc2) and np.abs(pr - pr2).max() < 1e-6
+
+
+def test_batch_rejects_cross_instance_edges():
+    g, vb = gx.batch_graph(4, scales=(5, 6), edge_factors=(4, 4), seed=1)
+    bad = vb.copy()
+    bad[2] = bad[2] + 3           # instance boundaries no longer match the edges
+    with engine_for(g) as e:
+        with pytest.raises(gx.GxError) as ei:
+            e.batch_run(bad)
+    assert ei.value.status == gx.GX_ERR_INVALID
