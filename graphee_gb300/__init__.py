@@ -69,6 +69,15 @@ class BatchTuning(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class WarmStats(C.Structure):
+    _fields_ = [("used_warm", C.c_int32), ("iterations", C.c_int32), ("resid_uniform_first", C.c_double),
+                ("resid_warm_first", C.c_double), ("resid_last", C.c_double), ("ms_features", C.c_double),
+                ("ms_mlp", C.c_double), ("ms_pagerank", C.c_double), ("ms_total", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 class IterStats(C.Structure):
     _fields_ = [("changed", C.c_int64), ("active", C.c_int64), ("shards_active", C.c_int32),
                 ("mode", C.c_int32), ("residual_l1", C.c_double), ("dangling", C.c_double),
@@ -114,6 +123,16 @@ def lib() -> C.CDLL:
         "gx_triangle_count": (C.c_int, [P, P, P]),
         "gx_ppr": (C.c_int, [P, I32, P, I32, D, P, P]),
         "gx_batch_tuning_default": (None, [P]),
+        "gx_mlp_num_params": (C.c_int32, []),
+        "gx_mlp_create": (C.c_int, [I32, U64, P]),
+        "gx_mlp_destroy": (C.c_int, [P]),
+        "gx_mlp_get_params": (C.c_int, [P, P, P]),
+        "gx_mlp_set_params": (C.c_int, [P, P, P]),
+        "gx_mlp_add_graph": (C.c_int, [P, P, I32, I32, D]),
+        "gx_mlp_train": (C.c_int, [P, I32, I32, D, P]),
+        "gx_mlp_grad": (C.c_int, [P, P, P, I32, P, P]),
+        "gx_mlp_predict": (C.c_int, [P, P, D, P, P, P]),
+        "gx_pagerank_warm": (C.c_int, [P, P, I32, D, D, P]),
         "gx_batch_run": (C.c_int, [P, I32, P, I32, I32, D, P, P, P, P, P, P]),
         "gx_batch_autotune": (C.c_int, [P, I32, P, I32, I32, C.c_char_p, P, P]),
     }
@@ -398,10 +417,73 @@ class Engine:
                                        C.byref(ms)), "gx_batch_autotune")
         return best.as_dict(), ms.value
 
+    def pagerank_warm(self, mlp: "MLP", max_iter=500, tolerance=1e-6, damping=0.85) -> dict:
+        """Standard PageRank to the L1 tolerance from the MLP's predicted start
+        (uniform start when the prediction's first step is worse)."""
+        ws = WarmStats()
+        _check(lib().gx_pagerank_warm(self._h, mlp._h, max_iter, tolerance, damping, C.byref(ws)),
+               "gx_pagerank_warm")
+        self.app = APP_PAGERANK_STD
+        return ws.as_dict()
+
     def iter_stats(self, step: int) -> dict:
         s = IterStats()
         _check(lib().gx_get_iter_stats(self._h, step, C.byref(s)), "gx_get_iter_stats")
         return s.as_dict()
+
+
+class MLP:
+    """The warm-start network (gx_mlp): 6 -> 64 -> 64 -> 1, BF16 weights."""
+
+    def __init__(self, device: int = 0, seed: int = 0):
+        self._h = C.c_void_p()
+        _check(lib().gx_mlp_create(device, seed & 0xFFFFFFFFFFFFFFFF, C.byref(self._h)), "gx_mlp_create")
+        self.n_params = int(lib().gx_mlp_num_params())
+
+    def close(self):
+        if self._h:
+            lib().gx_mlp_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def params(self):
+        p = np.empty(self.n_params, np.float32)
+        nrm = np.empty(12, np.float32)
+        _check(lib().gx_mlp_get_params(self._h, _ptr(p), _ptr(nrm)), "gx_mlp_get_params")
+        return p, nrm
+
+    def set_params(self, p=None, norm=None):
+        p = None if p is None else np.ascontiguousarray(p, np.float32)
+        norm = None if norm is None else np.ascontiguousarray(norm, np.float32)
+        _check(lib().gx_mlp_set_params(self._h, _ptr(p), _ptr(norm)), "gx_mlp_set_params")
+
+    def add_graph(self, engine: Engine, max_samples=65536, max_iter=300, tolerance=1e-9):
+        _check(lib().gx_mlp_add_graph(self._h, engine._h, max_samples, max_iter, tolerance), "gx_mlp_add_graph")
+
+    def train(self, epochs: int, batch: int = 4096, lr: float = 1e-3) -> float:
+        loss = C.c_double(0)
+        _check(lib().gx_mlp_train(self._h, epochs, batch, lr, C.byref(loss)), "gx_mlp_train")
+        return loss.value
+
+    def grad(self, x, t):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        g = np.empty(self.n_params, np.float32)
+        loss = C.c_double(0)
+        _check(lib().gx_mlp_grad(self._h, _ptr(x), _ptr(t), len(t), _ptr(g), C.byref(loss)), "gx_mlp_grad")
+        return g, loss.value
+
+    def predict(self, engine: Engine, damping=0.85):
+        out = np.empty(engine.V, np.float32)
+        mf, mm = C.c_double(0), C.c_double(0)
+        _check(lib().gx_mlp_predict(self._h, engine._h, damping, _ptr(out), C.byref(mf), C.byref(mm)),
+               "gx_mlp_predict")
+        return out, {"ms_features": mf.value, "ms_mlp": mm.value}
 
 
 # ------------------------------------------- the reference's app interface ----

@@ -74,6 +74,24 @@ def build_lib(force: bool = False) -> Path:
     return LIB
 
 
+APP = PKG / "gx_app"
+
+
+def build_apps() -> Path:
+    """The C++ app drivers (apps/gx_app.cpp over include/gx_graphps.hpp),
+    linked against libgx.so with an rpath to it."""
+    src = PKG / "apps" / "gx_app.cpp"
+    deps = [src, LIB, ROOT / "include" / "gx_graphps.hpp", ROOT / "include" / "gx.h"]
+    if APP.exists() and APP.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+        return APP
+    cmd = ["g++", "-O2", "-std=c++17", "-I", str(ROOT / "include"), str(src), "-o", str(APP),
+           "-L", str(PKG), "-lgx", "-Wl,-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"app build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return APP
+
+
 def build_oracle() -> None:
     """Compiles the oracle's CPU restatement; and the reference's own apps
     when the reference tree is present on this machine."""
@@ -90,6 +108,7 @@ def build_oracle() -> None:
 
 def build(force: bool = False) -> None:
     build_lib(force)
+    build_apps()
     build_oracle()
 
 

@@ -279,7 +279,9 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   c.shard_mask = ~0ull;
   // Initial values: init_vertex of the app, or the caller's values.
   int use_init = 0;
-  if (prm.use_init) {
+  if (e->device_init) {
+    use_init = 1;  // values already placed in d_val[0] on the device (warm start)
+  } else if (prm.use_init) {
     if (!e->has_init) return fail(GX_ERR_STATE, "gx_run: use_init set but gx_set_init was not called");
     GX_CUDA(cudaMemcpy(e->d_val[0], e->init_vals.data(), sizeof(T) * V, cudaMemcpyHostToDevice));
     use_init = 1;
@@ -291,13 +293,14 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
     for (int32_t v = 0; v < V; ++v) {
       if (e->outdeg[v] != 0) continue;
       ++n_dangling;
-      if (use_init) {
+      if (use_init && !e->device_init) {
         float x;
         memcpy(&x, &e->init_vals[v], sizeof(float));
         D += x;
       }
     }
     if (!use_init) D = static_cast<double>(n_dangling) * static_cast<double>(static_cast<float>(1.0 / V));
+    if (e->device_init) D = e->device_init_dangling;
     c.base = (1.0 - prm.damping) * c.inv_n + prm.damping * D * c.inv_n;
   }
   GX_CUDA(cudaMemcpyAsync(e->d_ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, e->s_comp));
@@ -769,15 +772,17 @@ gx_status gx_run(gx_engine* e, const gx_run_params* prm, gx_run_stats* stats) {
     if (stats) *stats = gx_run_stats{};
     return GX_OK;
   }
+  gx_status st = GX_ERR_INVALID;
   switch (kind) {
-    case K_PR_REF: return run_app<K_PR_REF>(e, p, stats);
-    case K_PR_STD: return run_app<K_PR_STD>(e, p, stats);
-    case K_SSSP_UNIT: return run_app<K_SSSP_UNIT>(e, p, stats);
-    case K_SSSP_W: return run_app<K_SSSP_W>(e, p, stats);
-    case K_CC: return run_app<K_CC>(e, p, stats);
-    case K_INDEG: return run_app<K_INDEG>(e, p, stats);
+    case K_PR_REF: st = run_app<K_PR_REF>(e, p, stats); break;
+    case K_PR_STD: st = run_app<K_PR_STD>(e, p, stats); break;
+    case K_SSSP_UNIT: st = run_app<K_SSSP_UNIT>(e, p, stats); break;
+    case K_SSSP_W: st = run_app<K_SSSP_W>(e, p, stats); break;
+    case K_CC: st = run_app<K_CC>(e, p, stats); break;
+    case K_INDEG: st = run_app<K_INDEG>(e, p, stats); break;
   }
-  return fail(GX_ERR_INVALID, "gx_run: unknown app");
+  e->device_init = false;
+  return st;
 }
 
 gx_status gx_get_values(gx_engine* e, void* host_out) {

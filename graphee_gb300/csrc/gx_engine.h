@@ -123,6 +123,9 @@ struct gx_engine {
 
   std::vector<uint32_t> init_vals;
   bool has_init = false;
+  bool device_init = false;          // next gx_run starts from d_val[0] as it is
+  double device_init_dangling = 0;   // PageRank STD: its dangling mass
+  double last_uniform_resid = 0;     // warm start: uniform start's first-step L1 residual
 
   // last run
   gx_app last_app = GX_APP_PAGERANK_REF;

@@ -201,6 +201,48 @@ gx_status gx_batch_autotune(gx_engine* e, int32_t n_inst, const int32_t* inst_vb
                             int32_t cc_max_iter, const char* table_path, gx_batch_tuning* best,
                             double* best_ms);
 
+/* ---- learned PageRank warm start (no reference counterpart) ----
+ * MLP 6 -> 64 -> 64 -> 1 (GELU, softplus output normalised to sum 1) over
+ * per-vertex degree features: log1p(indeg), log1p(outdeg), mean and max of
+ * in-neighbours' log1p(outdeg), log1p(2-hop in-degree sum), dangling flag.
+ * BF16 weights, FP32 accumulation; inference on the tensor cores. */
+typedef struct gx_mlp gx_mlp;
+
+typedef struct gx_warm_stats {
+  int32_t used_warm;            /* 0: fell back to the uniform start */
+  int32_t iterations;           /* supersteps to the tolerance (incl. the first) */
+  double resid_uniform_first;   /* L1 residual of one step from 1/N */
+  double resid_warm_first;      /* L1 residual of one step from the prediction */
+  double resid_last;
+  double ms_features, ms_mlp, ms_pagerank, ms_total;
+} gx_warm_stats;
+
+int32_t gx_mlp_num_params(void);
+gx_status gx_mlp_create(int32_t device, uint64_t seed, gx_mlp** out);
+gx_status gx_mlp_destroy(gx_mlp* m);
+/* params float[gx_mlp_num_params()] (FP32 master: W1[64][6], b1[64],
+ * W2[64][64], b2[64], w3[64], b3), norm float[12] (feature mean, 1/std). */
+gx_status gx_mlp_get_params(gx_mlp* m, float* params, float* norm);
+gx_status gx_mlp_set_params(gx_mlp* m, const float* params, const float* norm);
+/* Adds up to max_samples vertices of the engine's graph to the training
+ * set, with targets log(N * r_v) of standard PageRank run to `tolerance`. */
+gx_status gx_mlp_add_graph(gx_mlp* m, gx_engine* e, int32_t max_samples, int32_t max_iter,
+                           double tolerance);
+/* Adam on the squared error of log softplus(z) against the targets. */
+gx_status gx_mlp_train(gx_mlp* m, int32_t epochs, int32_t batch, double lr, double* final_loss);
+/* Gradient of the mean loss over n samples (raw features x[n][6], targets
+ * t[n]) at the current weights, float[gx_mlp_num_params()]. */
+gx_status gx_mlp_grad(gx_mlp* m, const float* x, const float* t, int32_t n, float* grad, double* loss);
+/* Predicted start vector (sums to 1) for the engine's graph, left on the
+ * device for gx_pagerank_warm; host_out (nullable) receives a copy. */
+gx_status gx_mlp_predict(gx_mlp* m, gx_engine* e, double damping, float* host_out, double* ms_features,
+                         double* ms_mlp);
+/* Standard PageRank to `tolerance` (L1 residual) from the MLP's start, or
+ * from the uniform start when the predicted start's first-step residual is
+ * worse than the uniform start's. */
+gx_status gx_pagerank_warm(gx_engine* e, gx_mlp* m, int32_t max_iter, double tolerance, double damping,
+                           gx_warm_stats* out);
+
 /* PageRank with the reference's semantics (GX_APP_PAGERANK_REF, default
  * tree-sum mode) over a CSC the caller already holds in device memory, for
  * callers that cannot allocate device memory themselves or let a library do

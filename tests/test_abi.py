@@ -49,3 +49,27 @@ def test_null_arguments_are_errors():
     assert L.gx_get_values(None, None) == gx.GX_ERR_INVALID
     assert "bad arguments" in L.gx_last_error().decode()
     assert L.gx_destroy(None) == gx.GX_OK
+
+
+def test_cpp_header_compiles():
+    import subprocess
+    src = "#include \"gx_graphps.hpp\"\nint main(){ gx::PagerankPS<float>* p = nullptr; (void)p; return 0; }\n"
+    r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-I", str(ROOT / "include"), "-x", "c++", "-"],
+                       input=src, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+def test_app_driver_reports_missing_device(tmp_path):
+    """Without a GPU the driver fails with an error status, not a crash."""
+    import subprocess
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    g = gx.rmat_graph(8, 4, seed=1, P=2)
+    d = gx.write_shards(g, tmp_path / "s")
+    app = gx.LIB_PATH.parent / "gx_app"
+    if not app.exists():
+        from graphee_gb300 import _build
+        _build.build_apps()
+    r = subprocess.run([str(app), "pagerank", d, str(g.V), "2", "5"], capture_output=True, text=True)
+    assert r.returncode == 1 and "no CUDA device" in r.stderr, r.stderr

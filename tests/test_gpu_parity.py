@@ -278,3 +278,24 @@ def test_batch_rejects_cross_instance_edges():
         with pytest.raises(gx.GxError) as ei:
             e.batch_run(bad)
     assert ei.value.status == gx.GX_ERR_INVALID
+
+
+def test_cpp_app_drivers_vs_oracle(tmp_path):
+    """The C++ GraphPS<T> mirror (include/gx_graphps.hpp) behind the
+    command-line drivers, on shards written in the reference layout."""
+    import subprocess
+    g = gx.rmat_graph(12, 16, seed=4, P=6)
+    d = gx.write_shards(g, tmp_path / "s")
+    app = str(gx.LIB_PATH.parent / "gx_app")
+    out = tmp_path / "pr.bin"
+    subprocess.run([app, "pagerank", d, str(g.V), str(g.P), "20", str(out)], check=True)
+    ref, _, _ = O.run(O.PAGERANK_REF, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 20)
+    vals = np.fromfile(out, np.float32)
+    assert np.abs(vals - ref).max() / ref.max() < 1e-5
+    subprocess.run([app, "sssp", d, str(g.V), str(g.P), "100", str(out), "0"], check=True)
+    ref, _, _ = O.run(O.SSSP, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 100, source=0)
+    assert np.array_equal(np.fromfile(out, np.int32), ref)
+    s = gx.rmat_graph(11, 8, seed=5, P=3, symmetric=True)
+    d2 = gx.write_shards(s, tmp_path / "t")
+    r = subprocess.run([app, "tc", d2, str(s.V), str(s.P), "0"], check=True, capture_output=True, text=True)
+    assert int(r.stdout.strip()) == O.triangles(s.V, s.off, s.col)
