@@ -36,6 +36,20 @@ SEED = 20240601
 SHARDS = 256
 
 
+def aggregate(ms_step: float, units_per_rank: float, dist=None, device=None):
+    """Replicas: the step time is the max over ranks, the work the sum.
+    Returns (max ms per step, total units per second)."""
+    if dist is None:
+        return ms_step, units_per_rank / (ms_step / 1000)
+    import torch
+    t = torch.tensor([ms_step, units_per_rank], dtype=torch.float64, device=device)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    tot = t.clone()
+    dist.all_reduce(tot, op=dist.ReduceOp.SUM)
+    return float(mx[0]), float(tot[1]) / (float(mx[0]) / 1000)
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -48,6 +62,10 @@ def parse():
     ap.add_argument("--cpu-iters", type=int, default=2, help="PageRank supersteps in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-sssp", action="store_true", help="skip the SSSP keys of the default run")
+    ap.add_argument("--workload", default="pagerank",
+                    choices=["pagerank", "cc_tc", "stream", "batch", "ppr", "warm"],
+                    help="pagerank = the headline run; the others measure the remaining configurations")
     return ap.parse_args()
 
 
@@ -223,13 +241,9 @@ def run_gx(args, rank, local_rank, world):
         barrier()
         wall = time.perf_counter() - t0
     clocks = clk.summary()
-    ms_step = dev_ms / args.steps
-    if dist is not None:
-        t = torch.tensor([ms_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_step = float(t.item())
     edges_per_step = g.E * args.iters
-    value = world * edges_per_step / (ms_step / 1000) / 1e9
+    ms_step, eps = aggregate(dev_ms / args.steps, float(edges_per_step), dist, "cuda")
+    value = eps / 1e9
 
     # Dominant kernel, timed live with CUDA events on the engine's stream.
     prof = gx.Engine(device=local_rank, profile=1)
@@ -255,14 +269,26 @@ def run_gx(args, rank, local_rank, world):
         torch.cuda.synchronize()
         if i > 0:
             e2e_s.append(time.perf_counter() - t1)
-    e2e_step = sum(e2e_s) / len(e2e_s)
-    if dist is not None:
-        t = torch.tensor([e2e_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_step = float(t.item())
+    e2e_step, e2e_eps = aggregate(sum(e2e_s) / len(e2e_s) * 1000, float(edges_per_step), dist, "cuda")
+    e2e_step /= 1000
     h2d = 4 * g.E + 8 * (g.V + 1) + 4 * g.V
     d2h = 4 * g.V
     assert np.isfinite(vals).all()
+
+    sssp = None
+    if not args.no_sssp:
+        g.weights = gx.edge_weights(7, g)
+        eng.set_weights(g.weights)
+        for _ in range(2):
+            eng.run(gx.APP_SSSP, 10000, source=0, weighted=True)
+        runs = [eng.run(gx.APP_SSSP, 10000, source=0, weighted=True) for _ in range(3)]
+        ms_s = sum(r["ms_total"] for r in runs) / len(runs)
+        scanned = runs[-1]["edges_scanned"]
+        launches += sum(r["kernel_launches"] for r in runs)
+        sssp = {"metric": "sssp_gteps", "value": g.E / (ms_s / 1000) / 1e9, "unit": "GTEPS (input edges / run)",
+                "scanned_gteps": scanned / (ms_s / 1000) / 1e9, "ms_per_run": ms_s,
+                "supersteps": runs[-1]["iterations"], "push_supersteps": runs[-1]["push_iterations"],
+                "weights": "uint32 in [1,255], seeded", "source": 0}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -278,14 +304,14 @@ def run_gx(args, rank, local_rank, world):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded R-MAT)",
                 "config": cfg,
-                "e2e": {"value": world * edges_per_step / e2e_step / 1e9, "unit": "GTEPS",
+                "e2e": {"value": e2e_eps / 1e9, "unit": "GTEPS",
                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "s_per_step": e2e_step},
                 "gpu_launches": launches,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                              "kernel": "pull_kernel<PAGERANK_REF>", "kernel_ms": pull_ms,
                              "algorithmic_bytes_per_launch": alg_bytes},
-                "cpu_baseline": cpu, "clocks": clocks, "wall_s_timed": wall,
+                "cpu_baseline": cpu, "clocks": clocks, "wall_s_timed": wall, "sssp": sssp,
                 "iterations_per_step": iters_done / args.steps}
         print(json.dumps(line), flush=True)
     eng.close()
@@ -294,11 +320,184 @@ def run_gx(args, rank, local_rank, world):
     return 0
 
 
+# ---------------------------------------------------------------------------
+# The other configurations (opt-in with --workload; one JSON line each).
+# ---------------------------------------------------------------------------
+
+def _line(metric, value, unit, args, config, **extra):
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic (seeded R-MAT)",
+         "config": config}
+    d.update(extra)
+    print(json.dumps(d), flush=True)
+
+
+def run_cc_tc(args):
+    import graphee_gb300 as gx
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import gx_oracle as O
+    t0 = time.time()
+    g = gx.rmat_graph(args.scale, args.edge_factor, seed=SEED, P=SHARDS, symmetric=True)
+    build_s = time.time() - t0
+    with gx.Engine() as e:
+        e.load(g)
+        for _ in range(args.warmup):
+            e.run(gx.APP_CC, 10000)
+        runs = [e.run(gx.APP_CC, 10000) for _ in range(args.steps)]
+        cc = e.values()
+        ms_cc = sum(r["ms_total"] for r in runs) / len(runs)
+        tri, st = e.triangle_count()
+        tri2, st2 = e.triangle_count()
+    t1 = time.perf_counter()
+    ref, ch, _ = O.run(O.CC, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 10000, threads=os.cpu_count())
+    cpu_s = time.perf_counter() - t1
+    cfg = {"workload": f"R-MAT scale {args.scale} edge factor {args.edge_factor}, symmetrised, deduplicated",
+           "vertices": g.V, "directed_entries": g.E, "graph_build_s": round(build_s, 1)}
+    _line("cc_gteps", g.E / (ms_cc / 1000) / 1e9, "GTEPS (input entries / run)", args, cfg, dtype="int32",
+          ms_per_run=ms_cc, supersteps=runs[-1]["iterations"], push_supersteps=runs[-1]["push_iterations"],
+          scanned_gteps=runs[-1]["edges_scanned"] / (ms_cc / 1000) / 1e9,
+          bit_exact_vs_oracle=bool(np.array_equal(cc, ref)), oracle_supersteps=len(ch),
+          cpu_baseline={"value": g.E * len(ch) / cpu_s / 1e9, "unit": "GTEPS (entries x supersteps / s)",
+                        "cores": os.cpu_count(), "kind": "port", "sample": "full CC run, same graph"},
+          triangles=tri, tc_ms=min(st["ms_total"], st2["ms_total"]), tc_repeatable=tri == tri2,
+          tc_work_edges=st["edges_scanned"])
+
+
+def run_stream(args):
+    import graphee_gb300 as gx
+    scale = args.scale if args.scale != 24 else 28
+    t0 = time.time()
+    g = gx.rmat_graph(scale, args.edge_factor, seed=SEED, P=256)
+    build_s = time.time() - t0
+    budget = 8 << 30
+    t1 = time.time()
+    e = gx.Engine(cache_budget_bytes=budget)
+    e.load(g)
+    load_s = time.time() - t1
+    e.run(gx.APP_PAGERANK_REF, 2)
+    pr = e.run(gx.APP_PAGERANK_REF, 10)
+    cfg = {"workload": f"R-MAT scale {scale} edge factor {args.edge_factor}, 256 shards, HBM shard cache 8 GiB, "
+                       "10 PageRank supersteps then weighted SSSP", "vertices": g.V, "edges": g.E,
+           "graph_build_s": round(build_s, 1), "load_s": round(load_s, 1)}
+    w = gx.edge_weights(7, g)
+    e.set_weights(w)
+    del w
+    ss = e.run(gx.APP_SSSP, 10000, source=0, weighted=True)
+    _line("pagerank_gteps_streamed", 10 * g.E / (pr["ms_total"] / 1000) / 1e9, "GTEPS", args, cfg, dtype="f32",
+          ms_per_superstep=pr["ms_total"] / 10, shards_resident=pr["shards_resident"],
+          h2d_gb_per_superstep=pr["h2d_bytes"] / 10 / 1e9, copy_ms=pr["ms_copy"], compute_ms=pr["ms_compute"],
+          overlap=pr["overlap"],
+          sssp={"gteps": g.E / (ss["ms_total"] / 1000) / 1e9, "ms": ss["ms_total"], "supersteps": ss["iterations"],
+                "h2d_gb": ss["h2d_bytes"] / 1e9, "overlap": ss["overlap"], "shards_streamed": ss["shards_streamed"]})
+    e.close()
+
+
+def run_batch(args):
+    import graphee_gb300 as gx
+    t0 = time.time()
+    g, vb = gx.batch_graph(2048, scales=(10, 17), edge_factors=(8, 32), seed=SEED)
+    build_s = time.time() - t0
+    n = len(vb) - 1
+    with gx.Engine() as e:
+        e.load(g)
+        table = ROOT / "profiles" / "batch_autotune_table.jsonl"
+        best, best_ms = e.batch_autotune(vb, pr_iters=30, cc_max_iter=1000, table_path=str(table))
+        for _ in range(args.warmup):
+            e.batch_run(vb, 30, 1000, tuning=best)
+        runs = [e.batch_run(vb, 30, 1000, tuning=best)[4] for _ in range(args.steps)]
+        ms_b = sum(r["ms_total"] for r in runs) / len(runs)
+        edges_b = runs[-1]["edges_scanned"]
+    # One engine launch sequence per instance (load excluded from the timing).
+    ms_sep = 0.0
+    edges_sep = 0
+    for i in range(n):
+        b, en = int(vb[i]), int(vb[i + 1])
+        sub = gx.Graph(en - b, g.off[b:en + 1] - g.off[b], g.col[g.off[b]:g.off[en]] - b, g.outdeg[b:en], 1)
+        with gx.Engine() as e1:
+            e1.load(sub)
+            a = e1.run(gx.APP_PAGERANK_REF, 30)
+            c = e1.run(gx.APP_CC, 1000)
+            ms_sep += a["ms_total"] + c["ms_total"]
+            edges_sep += a["edges_scanned"] + c["edges_scanned"]
+    cfg = {"workload": "2048 R-MAT instances, scale U{10..17}, edge factor U{8..32}, per-instance seeds; "
+                       "PageRank (reference semantics, 30 supersteps) then CC per instance",
+           "vertices": g.V, "edges": g.E, "graph_build_s": round(build_s, 1), "tuning": best}
+    _line("batch_instances_per_s", n / (ms_b / 1000), "instances/s", args, cfg, dtype="f32+int32",
+          ms_per_batch=ms_b, gteps=edges_b / (ms_b / 1000) / 1e9, gpu_launches=1,
+          separate={"instances_per_s": n / (ms_sep / 1000), "gteps": edges_sep / (ms_sep / 1000) / 1e9,
+                    "ms": ms_sep, "note": "one engine run (graph replay of its superstep kernels) per instance"},
+          speedup_vs_separate=ms_sep / ms_b)
+
+
+def run_ppr(args):
+    import graphee_gb300 as gx
+    g, build_s = build_graph(args)
+    rng = np.random.default_rng(SEED)
+    src = rng.integers(0, g.V, size=64).astype(np.int32)
+    with gx.Engine() as e:
+        e.load(g)
+        e.ppr(src, 2, fetch=False)
+        runs = [e.ppr(src, args.iters, fetch=False)[1] for _ in range(args.steps)]
+    ms = sum(r["ms_total"] for r in runs) / len(runs)
+    per_it = ms / args.iters
+    alg = 4 * g.E + 256 * g.E + 2 * 256 * g.V
+    peak, kind = measured_peak_hbm()
+    cfg = {"workload": f"personalized PageRank, 64 sources U[0,V), restart 0.15, R-MAT scale {args.scale}, "
+                       f"{args.iters} steps", "vertices": g.V, "edges": g.E}
+    _line("ppr_gteps", g.E * args.iters / (ms / 1000) / 1e9, "GTEPS (edges x steps / s, 64 columns each)", args,
+          cfg, dtype="f32", ms_per_step=per_it,
+          roofline={"bound": "hbm", "achieved": alg / (per_it / 1000) / 1e9, "peak": peak, "unit": "GB/s",
+                    "frac": alg / (per_it / 1000) / 1e9 / peak, "peak_source": kind})
+
+
+def run_warm(args):
+    import graphee_gb300 as gx
+    rng = np.random.default_rng(SEED)
+    t0 = time.time()
+    m = gx.MLP(seed=SEED)
+    for i in range(256):
+        s = int(rng.integers(16, 21))
+        ja, jb, jc = rng.uniform(-0.05, 0.05, size=3)
+        g = gx.rmat_graph(s, 16, seed=SEED + 17 * i, P=16, a=0.57 + ja, b=0.19 + jb, c=0.19 + jc)
+        with gx.Engine() as e:
+            e.load(g)
+            m.add_graph(e, max_samples=65536, max_iter=500, tolerance=1e-9)
+    prep_s = time.time() - t0
+    t1 = time.time()
+    loss = m.train(20, batch=8192, lr=2e-3)
+    train_s = time.time() - t1
+    evals = {}
+    for scale in (24, 26):
+        g = gx.rmat_graph(scale, 16, seed=SEED + 99991 + scale, P=256)
+        with gx.Engine() as e:
+            e.load(g)
+            e.run(gx.APP_PAGERANK_STD, 3)
+            uni = e.run(gx.APP_PAGERANK_STD, 1000, tolerance=1e-6)
+            e.pagerank_warm(m, 1000, tolerance=1e-6)
+            ws = e.pagerank_warm(m, 1000, tolerance=1e-6)
+        warm_ms = ws["ms_features"] + ws["ms_mlp"] + ws["ms_pagerank"]
+        evals[f"rmat{scale}"] = {"uniform_iters": uni["iterations"], "uniform_ms": uni["ms_total"],
+                                 "warm_iters": ws["iterations"], "warm_ms": warm_ms, "used_warm": ws["used_warm"],
+                                 "features_ms": ws["ms_features"], "mlp_ms": ws["ms_mlp"],
+                                 "resid_first_uniform": ws["resid_uniform_first"],
+                                 "resid_first_warm": ws["resid_warm_first"],
+                                 "time_ratio_uniform_over_warm": uni["ms_total"] / warm_ms}
+    cfg = {"workload": "warm start: 256 R-MAT training graphs (scale U{16..20}, a,b,c jittered +-0.05, 65536 "
+                       "sampled vertices each), standard PageRank to L1 < 1e-6 on held-out scale 24 and 26",
+           "train_prep_s": round(prep_s, 1), "train_s": round(train_s, 1), "final_loss": loss}
+    r24 = evals["rmat24"]
+    _line("warm_start_time_ratio", r24["time_ratio_uniform_over_warm"], "x (uniform time / warm time, scale 24)",
+          args, cfg, dtype="bf16 weights, f32 accumulate", evals=evals)
+
+
 def main():
     args = parse()
     rank, local_rank, world = dist_env()
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.workload != "pagerank":
+        return {"cc_tc": run_cc_tc, "stream": run_stream, "batch": run_batch, "ppr": run_ppr,
+                "warm": run_warm}[args.workload](args) or 0
     return run_gx(args, rank, local_rank, world)
 
 

@@ -1,0 +1,340 @@
+// Default pull kernel over the block layout (the engine re-lays each shard's
+// edges at load time; see build_blocks in gx_engine.cu).
+//
+// A block is one of
+//   light  : up to 256 vertices of in-degree <= kLightDegree, consecutive in
+//            id order within the shard, and their in-edges (<= kBlockEdges)
+//   medium : vertices of in-degree in (kLightDegree, heavy], packed up to
+//            kBlockEdges edges
+//   heavy  : one kBlockEdges-edge chunk of a vertex above `heavy`
+// with its edges (and weights), vertex ids and block-relative list starts
+// stored contiguously and 16-byte aligned.  A persistent CTA walks its
+// blocks (static stride) through two shared-memory stages: one thread
+// issues 1-D TMA bulk copies (cp.async.bulk + mbarrier complete_tx) for the
+// next block while the CTA gathers for the current one, so only the
+// data-dependent gathers remain on the critical path.
+//   light  : a thread per vertex folds its list in edge order, 8 gathers in
+//            flight (PageRank sums match the reference's order);
+//   medium : a warp per vertex, fixed xor-tree;
+//   heavy  : the CTA reduces the chunk in a fixed order; the last chunk's CTA
+//            folds the chunk partials in chunk order and applies.
+// Every mbarrier wait is bounded: on timeout the kernel records an error in
+// the control block and stops.
+#pragma once
+#include "gx_kernels.cuh"
+
+namespace gx {
+
+constexpr int kBlockEdges = 4096;
+constexpr int kBlockVerts = 256;
+constexpr int kLightDegree = 32;
+constexpr int kBlockThreads = 256;
+constexpr uint32_t kWaitSpins = 1u << 26;
+
+struct BlockDesc {
+  long long e_begin;  // first edge of the block in the block layout (multiple of 4)
+  int n_copy;         // edges copied (multiple of 4)
+  int n_real;         // edges in use
+  int first;          // light/medium: first index into vlist/loff (multiple of 4); heavy: heavy id
+  int count;          // light/medium: vertices; heavy: chunks of the vertex
+  int type;           // 0 light, 1 medium, 2 heavy chunk
+  int aux;            // heavy: chunk index
+  int shard;
+  int pad;
+};
+
+struct BlockArgs {
+  Ctl* ctl;
+  const BlockDesc* blocks;
+  int n_blocks;
+  const int32_t* colp;   // edges in block layout
+  const uint32_t* wp;    // weights in block layout (weighted SSSP)
+  const int32_t* vlist;  // vertex ids of light/medium blocks
+  const int32_t* loff;   // block-relative list starts
+  const int4* heavy;     // (v, n_chunks, partial base, shard)
+  const int32_t* outdeg;
+  void* val[2];
+  float* con[2];
+  void* partial;
+  unsigned int* hticket;
+  uint32_t* bm;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// 1-D bulk copy global -> shared, completing on `bar`; 16-byte aligned, size % 16 == 0.
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+template <int APP>
+constexpr int block_stage_bytes() {
+  return kBlockEdges * 4 * (APP == K_SSSP_W ? 2 : 1) + kBlockVerts * 4 * 2 + 64;
+}
+
+template <int APP>
+__device__ __forceinline__ void issue_block(const BlockArgs& a, int blk, unsigned char* stage, uint64_t* bar) {
+  const BlockDesc d = a.blocks[blk];
+  *reinterpret_cast<BlockDesc*>(stage) = d;
+  int32_t* col_s = reinterpret_cast<int32_t*>(stage + 64);
+  uint32_t* w_s = reinterpret_cast<uint32_t*>(stage + 64 + kBlockEdges * 4);
+  int32_t* vl_s = reinterpret_cast<int32_t*>(stage + 64 + kBlockEdges * 4 * (APP == K_SSSP_W ? 2 : 1));
+  int32_t* lo_s = vl_s + kBlockVerts;
+  uint32_t bytes = static_cast<uint32_t>(d.n_copy) * 4u * (APP == K_SSSP_W ? 2u : 1u);
+  const int nv = d.type < 2 ? ((d.count + 3) & ~3) : 0;
+  bytes += static_cast<uint32_t>(nv) * 8u;
+  mbar_expect_tx(bar, bytes);
+  if (d.n_copy > 0) {
+    tma_load_1d(col_s, a.colp + d.e_begin, static_cast<uint32_t>(d.n_copy) * 4u, bar);
+    if constexpr (APP == K_SSSP_W) tma_load_1d(w_s, a.wp + d.e_begin, static_cast<uint32_t>(d.n_copy) * 4u, bar);
+  }
+  if (nv > 0) {
+    tma_load_1d(vl_s, a.vlist + d.first, static_cast<uint32_t>(nv) * 4u, bar);
+    tma_load_1d(lo_s, a.loff + d.first, static_cast<uint32_t>(nv) * 4u, bar);
+  }
+}
+
+template <int APP>
+__device__ __forceinline__ typename AppTraits<APP>::T stage_value(const void* src_val, const float* src_con,
+                                                                  const int32_t* col_s, const uint32_t* w_s, int k) {
+  uint32_t wt = 0;
+  if constexpr (APP == K_SSSP_W) wt = w_s[k];
+  const int32_t u = col_s[k];
+  if constexpr (is_pr<APP>()) return __ldg(src_con + u);
+  else if constexpr (APP == K_SSSP_UNIT) return __ldg(static_cast<const int32_t*>(src_val) + u) + 1;
+  else if constexpr (APP == K_SSSP_W) return sat_add(__ldg(static_cast<const uint32_t*>(src_val) + u), wt);
+  else return __ldg(static_cast<const int32_t*>(src_val) + u);
+}
+
+// Lanes whose vertices share a bitmap word combine their bits; the lowest
+// such lane issues one atomicOr.
+__device__ __forceinline__ void set_active_bit(uint32_t* bm, int v, bool act) {
+  if (!__ballot_sync(0xffffffffu, act)) return;
+  const unsigned grp = __match_any_sync(0xffffffffu, v >> 5);
+  const unsigned bits = __reduce_or_sync(grp, act ? (1u << (v & 31)) : 0u);
+  if ((threadIdx.x & 31) == __ffs(grp) - 1 && bits) atomicOr(bm + (v >> 5), bits);
+}
+
+template <int APP>
+__global__ void __launch_bounds__(kBlockThreads, 3) pull_block_kernel(BlockArgs a) {
+  typedef typename AppTraits<APP>::T T;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  __shared__ uint64_t bar[2];
+  __shared__ T s_red[kBlockThreads / 32];
+  __shared__ int s_err;
+  Ctl* ctl = a.ctl;
+  const int done = ctl->done, mode = ctl->mode;
+  if (done || mode == MODE_PUSH) return;
+  ApplyCtx c;
+  c.step = ctl->step;
+  c.damping = ctl->damping;
+  c.inv_n = ctl->inv_n;
+  c.fx_scale = ctl->fx_scale;
+  c.base = ctl->base;
+  const int cur = ctl->cur;
+  const int group = ctl->shard_group;
+  const unsigned long long smask = ctl->shard_mask;
+  const bool selective = mode == MODE_SELECTIVE;
+  const void* src_val = cur ? a.val[1] : a.val[0];
+  void* dst_val = cur ? a.val[0] : a.val[1];
+  const float* src_con = cur ? a.con[1] : a.con[0];
+  float* dst_con = cur ? a.con[0] : a.con[1];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  constexpr int kStage = block_stage_bytes<APP>();
+  if (threadIdx.x == 0) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    s_err = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  LocalAcc la;
+  uint32_t parity[2] = {0, 0};
+  int st = 0;
+  int b = blockIdx.x;
+  if (threadIdx.x == 0 && b < a.n_blocks) issue_block<APP>(a, b, smem_raw, &bar[0]);
+  for (; b < a.n_blocks; b += gridDim.x) {
+    const int nb = b + gridDim.x;
+    if (threadIdx.x == 0 && nb < a.n_blocks) {
+      fence_proxy_async();
+      issue_block<APP>(a, nb, smem_raw + (st ^ 1) * kStage, &bar[st ^ 1]);
+    }
+    // Bounded wait for this block's copies.
+    uint32_t spins = 0;
+    bool ready = mbar_try_wait(&bar[st], parity[st]);
+    while (!ready && ++spins < kWaitSpins) ready = mbar_try_wait(&bar[st], parity[st]);
+    if (!ready) s_err = 1;
+    __syncthreads();
+    if (s_err) break;
+    parity[st] ^= 1u;
+    unsigned char* sp = smem_raw + st * kStage;
+    const BlockDesc d = *reinterpret_cast<const BlockDesc*>(sp);
+    const int32_t* col_s = reinterpret_cast<const int32_t*>(sp + 64);
+    const uint32_t* w_s = reinterpret_cast<const uint32_t*>(sp + 64 + kBlockEdges * 4);
+    const int32_t* vl_s = reinterpret_cast<const int32_t*>(sp + 64 + kBlockEdges * 4 * (APP == K_SSSP_W ? 2 : 1));
+    const int32_t* lo_s = vl_s + kBlockVerts;
+    const bool on = !selective || ((smask >> (d.shard / group)) & 1ull);
+    if (d.type == 0) {
+      // ---- light: thread per vertex ----
+      const int t = threadIdx.x;
+      const bool valid = t < d.count;
+      int v = 0;
+      T old = T(0);
+      int32_t od = 0;
+      int beg = 0, end = 0;
+      if (valid) {
+        v = vl_s[t];
+        beg = lo_s[t];
+        end = t + 1 < d.count ? lo_s[t + 1] : d.n_real;
+        old = static_cast<const T*>(src_val)[v];
+        if constexpr (is_pr<APP>()) od = a.outdeg[v];
+      }
+      bool act = false;
+      if (valid && !on) {
+        static_cast<T*>(dst_val)[v] = old;
+        if constexpr (is_pr<APP>()) dst_con[v] = src_con[v];
+      } else if (valid) {
+        T acc;
+        if constexpr (is_pr<APP>()) acc = 0.f;
+        else acc = old;
+        if constexpr (APP != K_INDEG) {
+          for (int k = beg; k < end; k += 8) {
+            T vals[8];
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+              vals[j] = k + j < end ? stage_value<APP>(src_val, src_con, col_s, w_s, k + j) : identity<APP>();
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+              if (k + j < end) acc = combine<APP>(acc, vals[j]);
+          }
+        } else {
+          acc = static_cast<T>(end - beg);
+        }
+        la.edges += end - beg;
+        act = apply_vertex<APP>(c, v, acc, old, od, dst_val, dst_con, la);
+      }
+      set_active_bit(a.bm, v, act);
+    } else if (d.type == 1) {
+      // ---- medium: warp per vertex ----
+      for (int j = wid; j < d.count; j += kBlockThreads / 32) {
+        const int v = vl_s[j];
+        const int beg = lo_s[j];
+        const int end = j + 1 < d.count ? lo_s[j + 1] : d.n_real;
+        const T old = static_cast<const T*>(src_val)[v];
+        if (!on) {
+          if (lane == 0) {
+            static_cast<T*>(dst_val)[v] = old;
+            if constexpr (is_pr<APP>()) dst_con[v] = src_con[v];
+          }
+          continue;
+        }
+        T acc = identity<APP>();
+        if constexpr (APP != K_INDEG) {
+          for (int k = beg + lane; k < end; k += 32)
+            acc = combine<APP>(acc, stage_value<APP>(src_val, src_con, col_s, w_s, k));
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc = combine<APP>(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+        }
+        if (lane == 0) {
+          T fin;
+          if constexpr (is_pr<APP>()) fin = acc;
+          else if constexpr (APP == K_INDEG) fin = static_cast<T>(end - beg);
+          else fin = combine<APP>(old, acc);
+          const int32_t od = is_pr<APP>() ? a.outdeg[v] : 0;
+          la.edges += end - beg;
+          if (apply_vertex<APP>(c, v, fin, old, od, dst_val, dst_con, la)) atomicOr(a.bm + (v >> 5), 1u << (v & 31));
+        }
+      }
+    } else {
+      // ---- heavy chunk: the whole CTA ----
+      const int4 H = a.heavy[d.first];
+      const int v = H.x;
+      if (!on) {
+        if (d.aux == 0 && threadIdx.x == 0) {
+          static_cast<T*>(dst_val)[v] = static_cast<const T*>(src_val)[v];
+          if constexpr (is_pr<APP>()) dst_con[v] = src_con[v];
+        }
+      } else {
+        T acc = identity<APP>();
+        if constexpr (APP != K_INDEG) {
+          for (int k = threadIdx.x; k < d.n_real; k += kBlockThreads)
+            acc = combine<APP>(acc, stage_value<APP>(src_val, src_con, col_s, w_s, k));
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) acc = combine<APP>(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+          if (lane == 0) s_red[wid] = acc;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+          T tot = identity<APP>();
+          if constexpr (APP != K_INDEG)
+            for (int i = 0; i < kBlockThreads / 32; ++i) tot = combine<APP>(tot, s_red[i]);
+          la.edges += d.n_real;
+          T* part = static_cast<T*>(a.partial);
+          bool last = H.y == 1;
+          if (!last) {
+            part[H.z + d.aux] = tot;
+            __threadfence();
+            last = atomicAdd(a.hticket + d.first, 1u) == static_cast<unsigned>(H.y) - 1;
+          }
+          if (last) {
+            __threadfence();
+            if (H.y > 1) {
+              const volatile T* vp = part;
+              tot = identity<APP>();
+              for (int i = 0; i < H.y; ++i) tot = combine<APP>(tot, vp[H.z + i]);
+              a.hticket[d.first] = 0;
+            }
+            const T old = static_cast<const T*>(src_val)[v];
+            const int32_t od = is_pr<APP>() ? a.outdeg[v] : 0;
+            T fin;
+            if constexpr (is_pr<APP>()) fin = tot;
+            else fin = combine<APP>(old, tot);
+            if (apply_vertex<APP>(c, v, fin, old, od, dst_val, dst_con, la)) atomicOr(a.bm + (v >> 5), 1u << (v & 31));
+          }
+        }
+      }
+    }
+    __syncthreads();  // the stage is free for the copy two blocks ahead
+    st ^= 1;
+  }
+  if (s_err && threadIdx.x == 0) {
+    atomicExch(&ctl->error, 1);
+    // Let copies already issued land before the CTA exits (bounded).
+    for (int s = 0; s < 2; ++s) {
+      uint32_t spins = 0;
+      while (!mbar_try_wait(&bar[s], parity[s]) && ++spins < kWaitSpins) {
+      }
+    }
+  }
+  __syncthreads();
+  flush_block(ctl, la);
+}
+
+}  // namespace gx
