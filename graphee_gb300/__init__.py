@@ -43,7 +43,7 @@ class Config(C.Structure):
                 ("selective_threshold", C.c_double), ("heavy_degree", C.c_int32), ("tile_edges", C.c_int32),
                 ("exact_order", C.c_int32),
                 ("push_sparse", C.c_int32), ("use_graph", C.c_int32), ("wait_limit", C.c_uint32),
-                ("verbose", C.c_int32), ("profile", C.c_int32)]
+                ("verbose", C.c_int32), ("profile", C.c_int32), ("layout", C.c_int32)]
 
 
 class RunParams(C.Structure):
@@ -119,6 +119,7 @@ def lib() -> C.CDLL:
         "gx_write_shards": (C.c_int, [C.c_char_p, I32, I32, P, P, P, P]),
         "gx_read_shards": (C.c_int, [C.c_char_p, I32, I32, P, P, P, P, P]),
         "gx_edge_weights": (C.c_int, [U64, I32, P, P, P]),
+        "gx_convert_edge_list": (C.c_int, [C.c_char_p, I32, I32, I32, C.c_char_p, P]),
         "gx_pagerank_noalloc": (C.c_int, [P, P, I64, I64, P, I32, I32, D, P, P, P]),
         "gx_triangle_count": (C.c_int, [P, P, P]),
         "gx_ppr": (C.c_int, [P, I32, P, I32, D, P, P]),
@@ -244,6 +245,18 @@ def write_shards(g: Graph, directory: str) -> str:
     _check(lib().gx_write_shards(d.encode(), g.V, g.P, _ptr(g.bounds), _ptr(g.off), _ptr(g.col), _ptr(g.outdeg)),
            "gx_write_shards")
     return d
+
+
+def convert_edge_list(path: str, V: int, P: int, directory: str, flags=BUILD_DROP_SELF | BUILD_DEDUP) -> int:
+    """Text edge list ("src dst" lines) -> the reference's shard directory."""
+    d = str(directory)
+    if not d.endswith("/"):
+        d += "/"
+    os.makedirs(d, exist_ok=True)
+    n = C.c_int64(0)
+    _check(lib().gx_convert_edge_list(str(path).encode(), V, P, flags, d.encode(), C.byref(n)),
+           "gx_convert_edge_list")
+    return n.value
 
 
 def read_shards(directory: str, V: int, P: int) -> Graph:

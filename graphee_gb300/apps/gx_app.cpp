@@ -7,6 +7,7 @@
 //   gx_app sssp     <shard_dir/> <V> <P> <max_iter> [out.bin] [source]
 //   gx_app cc       <shard_dir/> <V> <P> <max_iter> [out.bin]
 //   gx_app tc       <shard_dir/> <V> <P> 0          (symmetric shards)
+//   gx_app convert  <edges.tsv> <V> <P> <out_dir/>  (edge list -> shards)
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -34,7 +35,10 @@ static int run_app(App& app, int argc, char** argv, const char* name) {
 
 int main(int argc, char** argv) {
   if (argc < 6) {
-    fprintf(stderr, "usage: %s pagerank|sssp|cc|tc <shard_dir/> <V> <P> <max_iter> [out.bin] [source]\n", argv[0]);
+    fprintf(stderr,
+            "usage: %s pagerank|sssp|cc|tc <shard_dir/> <V> <P> <max_iter> [out.bin] [source]\n"
+            "       %s convert <edges.tsv> <V> <P> <out_dir/>\n",
+            argv[0], argv[0]);
     return 2;
   }
   const std::string app = argv[1];
@@ -51,6 +55,14 @@ int main(int argc, char** argv) {
     if (app == "cc") {
       gx::CcPS<int32_t> pg;
       return run_app(pg, argc, argv, "cc");
+    }
+    if (app == "convert") {
+      int64_t kept = 0;
+      gx::check(gx_convert_edge_list(argv[2], atoi(argv[3]), atoi(argv[4]), GX_BUILD_DROP_SELF | GX_BUILD_DEDUP,
+                                     argv[5], &kept),
+                "gx_convert_edge_list");
+      printf("%lld\n", static_cast<long long>(kept));
+      return 0;
     }
     if (app == "tc") {
       gx_engine* e = nullptr;

@@ -1,23 +1,28 @@
-// Default pull kernel over the block layout (the engine re-lays each shard's
-// edges at load time; see build_blocks in gx_engine.cu).
+// Pull kernel over the block layout, selected by gx_config.layout = 1 (the
+// engine then re-lays each shard's edges at load time; see build_blocks in
+// gx_engine.cu).  The default layout is the warp work units of
+// gx_kernels.cuh, which measured faster on R-MAT inputs.
 //
 // A block is one of
-//   light  : up to 256 vertices of in-degree <= kLightDegree, consecutive in
+//   light  : up to 32 vertices of in-degree <= kLightDegree, consecutive in
 //            id order within the shard, and their in-edges (<= kBlockEdges)
-//   medium : vertices of in-degree in (kLightDegree, heavy], packed up to
-//            kBlockEdges edges
-//   heavy  : one kBlockEdges-edge chunk of a vertex above `heavy`
+//   medium : vertices of in-degree in (kLightDegree, kBlockEdges], packed
+//            up to kBlockEdges edges
+//   heavy  : one kBlockEdges-edge chunk of a longer list
 // with its edges (and weights), vertex ids and block-relative list starts
-// stored contiguously and 16-byte aligned.  A persistent CTA walks its
-// blocks (static stride) through two shared-memory stages: one thread
-// issues 1-D TMA bulk copies (cp.async.bulk + mbarrier complete_tx) for the
-// next block while the CTA gathers for the current one, so only the
-// data-dependent gathers remain on the critical path.
-//   light  : a thread per vertex folds its list in edge order, 8 gathers in
-//            flight (PageRank sums match the reference's order);
-//   medium : a warp per vertex, fixed xor-tree;
-//   heavy  : the CTA reduces the chunk in a fixed order; the last chunk's CTA
-//            folds the chunk partials in chunk order and applies.
+// stored contiguously and 16-byte aligned.  Every warp of a persistent grid
+// walks its own blocks (static stride) through its own two shared-memory
+// stages: lane 0 issues the 1-D TMA bulk copies (cp.async.bulk + mbarrier
+// complete_tx) of the next block while the warp gathers for the current
+// one, and no warp ever waits for another, so only the data-dependent
+// gathers remain on the critical path.
+// Each block is then two phases: all lanes issue every gather of the block at
+// once (up to 16 per lane) into a per-warp shared-memory value buffer; then
+//   light/medium : a lane per vertex folds its slice of the buffer in edge
+//                  order (the reference's summation order, so light and
+//                  medium vertices match the reference bit for bit);
+//   heavy        : a fixed-shape tree over the chunk; the warp that finishes
+//                  a vertex's last chunk folds the chunk partials in order.
 // Every mbarrier wait is bounded: on timeout the kernel records an error in
 // the control block and stops.
 #pragma once
@@ -25,10 +30,11 @@
 
 namespace gx {
 
-constexpr int kBlockEdges = 4096;
-constexpr int kBlockVerts = 256;
+constexpr int kBlockEdges = 512;
+constexpr int kBlockVerts = 32;
 constexpr int kLightDegree = 32;
 constexpr int kBlockThreads = 256;
+constexpr int kBlockWarps = kBlockThreads / 32;
 constexpr uint32_t kWaitSpins = 1u << 26;
 
 struct BlockDesc {
@@ -142,13 +148,15 @@ __device__ __forceinline__ void set_active_bit(uint32_t* bm, int v, bool act) {
   if ((threadIdx.x & 31) == __ffs(grp) - 1 && bits) atomicOr(bm + (v >> 5), bits);
 }
 
+#ifndef GX_BLOCK_MIN_BLOCKS
+#define GX_BLOCK_MIN_BLOCKS 3
+#endif
+
 template <int APP>
-__global__ void __launch_bounds__(kBlockThreads, 3) pull_block_kernel(BlockArgs a) {
+__global__ void __launch_bounds__(kBlockThreads, GX_BLOCK_MIN_BLOCKS) pull_block_kernel(BlockArgs a) {
   typedef typename AppTraits<APP>::T T;
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ uint64_t bar[2];
-  __shared__ T s_red[kBlockThreads / 32];
-  __shared__ int s_err;
+  __shared__ uint64_t bar[kBlockWarps][2];
   Ctl* ctl = a.ctl;
   const int done = ctl->done, mode = ctl->mode;
   if (done || mode == MODE_PUSH) return;
@@ -168,168 +176,144 @@ __global__ void __launch_bounds__(kBlockThreads, 3) pull_block_kernel(BlockArgs 
   float* dst_con = cur ? a.con[0] : a.con[1];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   constexpr int kStage = block_stage_bytes<APP>();
-  if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
-    s_err = 0;
+  // Per warp: two copy stages, then one buffer of gathered values.
+  unsigned char* wsm = smem_raw + static_cast<size_t>(wid) * (2 * kStage + kBlockEdges * 4);
+  T* vbuf = reinterpret_cast<T*>(wsm + 2 * kStage);
+  uint64_t* wbar = bar[wid];
+  if (lane == 0) {
+    mbar_init(&wbar[0], 1);
+    mbar_init(&wbar[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  __syncthreads();
+  __syncwarp();
   LocalAcc la;
   uint32_t parity[2] = {0, 0};
   int st = 0;
-  int b = blockIdx.x;
-  if (threadIdx.x == 0 && b < a.n_blocks) issue_block<APP>(a, b, smem_raw, &bar[0]);
-  for (; b < a.n_blocks; b += gridDim.x) {
-    const int nb = b + gridDim.x;
-    if (threadIdx.x == 0 && nb < a.n_blocks) {
+  bool err = false;
+  const int gw = blockIdx.x * kBlockWarps + wid;
+  const int nw = gridDim.x * kBlockWarps;
+  int b = gw;
+  if (lane == 0 && b < a.n_blocks) issue_block<APP>(a, b, wsm, &wbar[0]);
+  for (; b < a.n_blocks; b += nw) {
+    const int nb = b + nw;
+    if (lane == 0 && nb < a.n_blocks) {
       fence_proxy_async();
-      issue_block<APP>(a, nb, smem_raw + (st ^ 1) * kStage, &bar[st ^ 1]);
+      issue_block<APP>(a, nb, wsm + (st ^ 1) * kStage, &wbar[st ^ 1]);
     }
     // Bounded wait for this block's copies.
     uint32_t spins = 0;
-    bool ready = mbar_try_wait(&bar[st], parity[st]);
-    while (!ready && ++spins < kWaitSpins) ready = mbar_try_wait(&bar[st], parity[st]);
-    if (!ready) s_err = 1;
-    __syncthreads();
-    if (s_err) break;
+    bool ready = mbar_try_wait(&wbar[st], parity[st]);
+    while (!ready && ++spins < kWaitSpins) ready = mbar_try_wait(&wbar[st], parity[st]);
+    if (!__all_sync(0xffffffffu, ready)) {
+      err = true;
+      break;
+    }
     parity[st] ^= 1u;
-    unsigned char* sp = smem_raw + st * kStage;
+    const unsigned char* sp = wsm + st * kStage;
     const BlockDesc d = *reinterpret_cast<const BlockDesc*>(sp);
     const int32_t* col_s = reinterpret_cast<const int32_t*>(sp + 64);
     const uint32_t* w_s = reinterpret_cast<const uint32_t*>(sp + 64 + kBlockEdges * 4);
     const int32_t* vl_s = reinterpret_cast<const int32_t*>(sp + 64 + kBlockEdges * 4 * (APP == K_SSSP_W ? 2 : 1));
     const int32_t* lo_s = vl_s + kBlockVerts;
     const bool on = !selective || ((smask >> (d.shard / group)) & 1ull);
-    if (d.type == 0) {
-      // ---- light: thread per vertex ----
-      const int t = threadIdx.x;
-      const bool valid = t < d.count;
-      int v = 0;
-      T old = T(0);
-      int32_t od = 0;
-      int beg = 0, end = 0;
+    // Per-lane vertex of a light/medium block, loaded before the gathers.
+    const bool valid = d.type < 2 && lane < d.count;
+    int v = 0, beg = 0, end = 0;
+    T old = T(0);
+    int32_t od = 0;
+    if (valid) {
+      v = vl_s[lane];
+      beg = lo_s[lane];
+      end = lane + 1 < d.count ? lo_s[lane + 1] : d.n_real;
+      old = static_cast<const T*>(src_val)[v];
+      if constexpr (is_pr<APP>()) od = a.outdeg[v];
+    }
+    if (!on) {
       if (valid) {
-        v = vl_s[t];
-        beg = lo_s[t];
-        end = t + 1 < d.count ? lo_s[t + 1] : d.n_real;
-        old = static_cast<const T*>(src_val)[v];
-        if constexpr (is_pr<APP>()) od = a.outdeg[v];
-      }
-      bool act = false;
-      if (valid && !on) {
         static_cast<T*>(dst_val)[v] = old;
         if constexpr (is_pr<APP>()) dst_con[v] = src_con[v];
-      } else if (valid) {
+      }
+      if (d.type == 2 && d.aux == 0 && lane == 0) {
+        const int hv = a.heavy[d.first].x;
+        static_cast<T*>(dst_val)[hv] = static_cast<const T*>(src_val)[hv];
+        if constexpr (is_pr<APP>()) dst_con[hv] = src_con[hv];
+      }
+      __syncwarp();
+      st ^= 1;
+      continue;
+    }
+    // Phase 1: every gather of the block in flight at once (16 per lane).
+    {
+      T vals[kBlockEdges / 32];
+#pragma unroll
+      for (int j = 0; j < kBlockEdges / 32; ++j) {
+        const int k = lane + 32 * j;
+        vals[j] = k < d.n_real ? stage_value<APP>(src_val, src_con, col_s, w_s, k) : identity<APP>();
+      }
+#pragma unroll
+      for (int j = 0; j < kBlockEdges / 32; ++j) vbuf[lane + 32 * j] = vals[j];
+    }
+    __syncwarp();
+    // Phase 2: fold.
+    if (d.type < 2) {
+      // Lane per vertex, in edge order (the reference's summation order).
+      bool act = false;
+      if (valid) {
         T acc;
         if constexpr (is_pr<APP>()) acc = 0.f;
         else acc = old;
-        if constexpr (APP != K_INDEG) {
-          for (int k = beg; k < end; k += 8) {
-            T vals[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j)
-              vals[j] = k + j < end ? stage_value<APP>(src_val, src_con, col_s, w_s, k + j) : identity<APP>();
-#pragma unroll
-            for (int j = 0; j < 8; ++j)
-              if (k + j < end) acc = combine<APP>(acc, vals[j]);
-          }
-        } else {
-          acc = static_cast<T>(end - beg);
-        }
+#pragma unroll 4
+        for (int k = beg; k < end; ++k) acc = combine<APP>(acc, vbuf[k]);
         la.edges += end - beg;
         act = apply_vertex<APP>(c, v, acc, old, od, dst_val, dst_con, la);
       }
       set_active_bit(a.bm, v, act);
-    } else if (d.type == 1) {
-      // ---- medium: warp per vertex ----
-      for (int j = wid; j < d.count; j += kBlockThreads / 32) {
-        const int v = vl_s[j];
-        const int beg = lo_s[j];
-        const int end = j + 1 < d.count ? lo_s[j + 1] : d.n_real;
-        const T old = static_cast<const T*>(src_val)[v];
-        if (!on) {
-          if (lane == 0) {
-            static_cast<T*>(dst_val)[v] = old;
-            if constexpr (is_pr<APP>()) dst_con[v] = src_con[v];
-          }
-          continue;
-        }
-        T acc = identity<APP>();
-        if constexpr (APP != K_INDEG) {
-          for (int k = beg + lane; k < end; k += 32)
-            acc = combine<APP>(acc, stage_value<APP>(src_val, src_con, col_s, w_s, k));
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) acc = combine<APP>(acc, __shfl_xor_sync(0xffffffffu, acc, o));
-        }
-        if (lane == 0) {
-          T fin;
-          if constexpr (is_pr<APP>()) fin = acc;
-          else if constexpr (APP == K_INDEG) fin = static_cast<T>(end - beg);
-          else fin = combine<APP>(old, acc);
-          const int32_t od = is_pr<APP>() ? a.outdeg[v] : 0;
-          la.edges += end - beg;
-          if (apply_vertex<APP>(c, v, fin, old, od, dst_val, dst_con, la)) atomicOr(a.bm + (v >> 5), 1u << (v & 31));
-        }
-      }
     } else {
-      // ---- heavy chunk: the whole CTA ----
-      const int4 H = a.heavy[d.first];
-      const int v = H.x;
-      if (!on) {
-        if (d.aux == 0 && threadIdx.x == 0) {
-          static_cast<T*>(dst_val)[v] = static_cast<const T*>(src_val)[v];
-          if constexpr (is_pr<APP>()) dst_con[v] = src_con[v];
-        }
-      } else {
-        T acc = identity<APP>();
-        if constexpr (APP != K_INDEG) {
-          for (int k = threadIdx.x; k < d.n_real; k += kBlockThreads)
-            acc = combine<APP>(acc, stage_value<APP>(src_val, src_con, col_s, w_s, k));
+      // Heavy chunk: fixed-shape tree over the chunk, then chunk partials in order.
+      T acc = identity<APP>();
 #pragma unroll
-          for (int o = 16; o > 0; o >>= 1) acc = combine<APP>(acc, __shfl_xor_sync(0xffffffffu, acc, o));
-          if (lane == 0) s_red[wid] = acc;
+      for (int j = 0; j < kBlockEdges / 32; ++j) acc = combine<APP>(acc, vbuf[lane + 32 * j]);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc = combine<APP>(acc, __shfl_xor_sync(0xffffffffu, acc, o));
+      if (lane == 0) {
+        const int4 H = a.heavy[d.first];
+        const int hv = H.x;
+        T tot = acc;
+        la.edges += d.n_real;
+        T* part = static_cast<T*>(a.partial);
+        bool last = H.y == 1;
+        if (!last) {
+          part[H.z + d.aux] = tot;
+          __threadfence();
+          last = atomicAdd(a.hticket + d.first, 1u) == static_cast<unsigned>(H.y) - 1;
         }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-          T tot = identity<APP>();
-          if constexpr (APP != K_INDEG)
-            for (int i = 0; i < kBlockThreads / 32; ++i) tot = combine<APP>(tot, s_red[i]);
-          la.edges += d.n_real;
-          T* part = static_cast<T*>(a.partial);
-          bool last = H.y == 1;
-          if (!last) {
-            part[H.z + d.aux] = tot;
-            __threadfence();
-            last = atomicAdd(a.hticket + d.first, 1u) == static_cast<unsigned>(H.y) - 1;
+        if (last) {
+          __threadfence();
+          if (H.y > 1) {
+            const volatile T* vp = part;
+            tot = identity<APP>();
+            for (int i = 0; i < H.y; ++i) tot = combine<APP>(tot, vp[H.z + i]);
+            a.hticket[d.first] = 0;
           }
-          if (last) {
-            __threadfence();
-            if (H.y > 1) {
-              const volatile T* vp = part;
-              tot = identity<APP>();
-              for (int i = 0; i < H.y; ++i) tot = combine<APP>(tot, vp[H.z + i]);
-              a.hticket[d.first] = 0;
-            }
-            const T old = static_cast<const T*>(src_val)[v];
-            const int32_t od = is_pr<APP>() ? a.outdeg[v] : 0;
-            T fin;
-            if constexpr (is_pr<APP>()) fin = tot;
-            else fin = combine<APP>(old, tot);
-            if (apply_vertex<APP>(c, v, fin, old, od, dst_val, dst_con, la)) atomicOr(a.bm + (v >> 5), 1u << (v & 31));
-          }
+          const T hold = static_cast<const T*>(src_val)[hv];
+          const int32_t hod = is_pr<APP>() ? a.outdeg[hv] : 0;
+          T fin;
+          if constexpr (is_pr<APP>()) fin = tot;
+          else fin = combine<APP>(hold, tot);
+          if (apply_vertex<APP>(c, hv, fin, hold, hod, dst_val, dst_con, la))
+            atomicOr(a.bm + (hv >> 5), 1u << (hv & 31));
         }
       }
     }
-    __syncthreads();  // the stage is free for the copy two blocks ahead
+    __syncwarp();  // stage and value buffer free for the next block
     st ^= 1;
   }
-  if (s_err && threadIdx.x == 0) {
+  if (err && lane == 0) {
     atomicExch(&ctl->error, 1);
-    // Let copies already issued land before the CTA exits (bounded).
-    for (int s = 0; s < 2; ++s) {
+    // Let this warp's issued copies land before it exits (bounded).
+    for (int s2 = 0; s2 < 2; ++s2) {
       uint32_t spins = 0;
-      while (!mbar_try_wait(&bar[s], parity[s]) && ++spins < kWaitSpins) {
+      while (!mbar_try_wait(&wbar[s2], parity[s2]) && ++spins < kWaitSpins) {
       }
     }
   }

@@ -501,12 +501,13 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
 
   void (*pull)(PullArgs) = e->cfg.exact_order ? pull_kernel<APP, true> : pull_kernel<APP, false>;
   const int grid_pull = occupancy_grid<APP>(e, reinterpret_cast<const void*>(pull));
-  // Default resident path: the block-layout kernel (TMA-staged blocks).
-  const bool use_blocks = e->all_resident && e->blocks_ready && !e->cfg.exact_order && APP != K_INDEG &&
+  // Block layout (config.layout = 1): the TMA-staged block kernel.
+  const bool use_blocks = e->cfg.layout == 1 && e->all_resident && e->blocks_ready && !e->cfg.exact_order &&
+                          APP != K_INDEG &&
                           (APP != K_SSSP_W || e->d_wp != nullptr);
   BlockArgs ba{};
   int grid_block = 0;
-  const size_t block_smem = 2 * static_cast<size_t>(block_stage_bytes<APP>());
+  const size_t block_smem = (2 * static_cast<size_t>(block_stage_bytes<APP>()) + kBlockEdges * 4) * kBlockWarps;
   if (use_blocks) {
     GX_CUDA(cudaFuncSetAttribute(pull_block_kernel<APP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  static_cast<int>(block_smem)));
@@ -747,6 +748,7 @@ void gx_config_default(gx_config* cfg) {
   cfg->wait_limit = 1u << 22;
   cfg->verbose = 0;
   cfg->profile = 0;
+  cfg->layout = 0;
 }
 
 void gx_run_params_default(gx_run_params* p, gx_app app) {
@@ -865,7 +867,7 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   GX_TRY(plan_shards(e));
   GX_TRY(build_signatures(e));
   if (e->all_resident) {
-    GX_TRY(build_blocks(e, e->h_col));
+    if (e->cfg.layout == 1) GX_TRY(build_blocks(e, e->h_col));
     cudaFreeHost(e->h_col);
     e->h_col = nullptr;
   }

@@ -391,6 +391,78 @@ gx_status gx_read_shards(const char* dir, int32_t V, int32_t P, int32_t* bounds,
   return GX_OK;
 }
 
+gx_status gx_convert_edge_list(const char* path, int32_t V, int32_t P, int32_t flags, const char* out_dir,
+                               int64_t* n_edges_out) {
+  if (!path || !out_dir || V < 1 || P < 1) return fail(GX_ERR_INVALID, "gx_convert_edge_list: bad arguments");
+  FILE* f = fopen(path, "rb");
+  if (!f) return fail(GX_ERR_IO, "cannot open %s: %s", path, strerror(errno));
+  fseek(f, 0, SEEK_END);
+  const long size = ftell(f);
+  fseek(f, 0, SEEK_SET);
+  std::string text(static_cast<size_t>(size > 0 ? size : 0), '\0');
+  if (size > 0 && fread(&text[0], 1, static_cast<size_t>(size), f) != static_cast<size_t>(size)) {
+    fclose(f);
+    return fail(GX_ERR_IO, "%s: short read", path);
+  }
+  fclose(f);
+  // Split at line starts so threads parse independent ranges; '#' and '%'
+  // lines are comments.  Each line holds "src dst" (whitespace separated),
+  // the input format of GraphMP/tools/format_spark.py:51-53,111-113.
+  const int nt = omp_get_max_threads();
+  std::vector<size_t> cut(nt + 1, text.size());
+  cut[0] = 0;
+  for (int t = 1; t < nt; ++t) {
+    size_t c = text.size() * t / nt;
+    while (c < text.size() && text[c - 1] != '\n') ++c;
+    cut[t] = c;
+  }
+  std::vector<std::vector<int32_t>> srcs(nt), dsts(nt);
+  std::atomic<int> bad{0};
+#pragma omp parallel num_threads(nt)
+  {
+    const int t = omp_get_thread_num();
+    const char* p = text.data() + cut[t];
+    const char* end = text.data() + cut[t + 1];
+    while (p < end) {
+      const char* eol = static_cast<const char*>(memchr(p, '\n', end - p));
+      if (!eol) eol = end;
+      const char* q = p;
+      while (q < eol && (*q == ' ' || *q == '\t' || *q == '\r')) ++q;
+      if (q < eol && *q != '#' && *q != '%') {
+        char* e1 = nullptr;
+        const long long a = strtoll(q, &e1, 10);
+        char* e2 = nullptr;
+        const long long b = strtoll(e1, &e2, 10);
+        if (e1 == q || e2 == e1 || a < 0 || b < 0 || a >= V || b >= V) {
+          bad.store(1);
+        } else {
+          srcs[t].push_back(static_cast<int32_t>(a));
+          dsts[t].push_back(static_cast<int32_t>(b));
+        }
+      }
+      p = eol + 1;
+    }
+  }
+  if (bad.load()) return fail(GX_ERR_FORMAT, "%s: a line is not \"src dst\" with ids in [0, %d)", path, V);
+  std::vector<int32_t> src, dst;
+  for (int t = 0; t < nt; ++t) {
+    src.insert(src.end(), srcs[t].begin(), srcs[t].end());
+    dst.insert(dst.end(), dsts[t].begin(), dsts[t].end());
+  }
+  const int64_t n = static_cast<int64_t>(src.size());
+  std::vector<int64_t> off(static_cast<size_t>(V) + 1);
+  std::vector<int32_t> col(static_cast<size_t>(flags & GX_BUILD_SYMMETRIZE ? 2 * n : n) + 1);
+  int64_t E = 0;
+  gx_status st = gx_build_csc(V, n, src.data(), dst.data(), flags, off.data(), col.data(), &E);
+  if (st != GX_OK) return st;
+  std::vector<int32_t> outdeg(static_cast<size_t>(V)), bounds(static_cast<size_t>(P) + 1);
+  if ((st = gx_out_degree(V, off.data(), col.data(), outdeg.data())) != GX_OK) return st;
+  if ((st = gx_partition_bounds(V, off.data(), P, bounds.data())) != GX_OK) return st;
+  if ((st = gx_write_shards(out_dir, V, P, bounds.data(), off.data(), col.data(), outdeg.data())) != GX_OK) return st;
+  if (n_edges_out) *n_edges_out = E;
+  return GX_OK;
+}
+
 gx_status gx_edge_weights(uint64_t seed, int32_t V, const int64_t* off, const int32_t* col, uint32_t* w) {
   if (V < 0 || !off || (off[V] > 0 && (!col || !w))) return fail(GX_ERR_INVALID, "gx_edge_weights: bad arguments");
 #pragma omp parallel for schedule(dynamic, 4096)

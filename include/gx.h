@@ -75,6 +75,8 @@ typedef struct gx_config {
   uint32_t wait_limit;         /* iteration cap of every device spin-wait (default 1<<22) */
   int32_t verbose;             /* per-iteration log lines on stderr (default 0) */
   int32_t profile;             /* time every pull launch with CUDA events (default 0) */
+  int32_t layout;              /* resident pull layout: 0 = warp work units (default), 1 = TMA-staged
+                                  blocks (edges re-laid per shard, cp.async.bulk double buffering) */
 } gx_config;
 
 typedef struct gx_run_params {
@@ -300,6 +302,13 @@ gx_status gx_write_shards(const char* dir, int32_t V, int32_t P, const int32_t* 
  * Call first with off/col NULL to get *E_out; then with buffers. */
 gx_status gx_read_shards(const char* dir, int32_t V, int32_t P, int32_t* bounds,
                          int64_t* off, int32_t* col, int32_t* outdeg, int64_t* E_out);
+
+/* Edge-list text file ("src dst" per line, '#' or '%' comments) to the
+ * reference's shard directory: replaces the offline Spark job
+ * (GraphMP/tools/format_spark.py), with the same edge-balanced partition
+ * rule.  flags as gx_build_csc; *n_edges_out receives the edges kept. */
+gx_status gx_convert_edge_list(const char* path, int32_t V, int32_t P, int32_t flags, const char* out_dir,
+                               int64_t* n_edges_out);
 
 /* Seeded SSSP weights in [1,255], a pure function of (seed, u, v). */
 gx_status gx_edge_weights(uint64_t seed, int32_t V, const int64_t* off, const int32_t* col,

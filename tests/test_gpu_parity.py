@@ -53,6 +53,33 @@ def test_pagerank_default_mode_vs_reference(golden_cases):
         e.close()
 
 
+def test_block_layout_vs_reference(golden_cases):
+    """The TMA-staged block layout (config.layout = 1): SSSP/CC bit-exact,
+    PageRank bit-exact wherever no vertex has more than 512 in-edges (every
+    list up to 512 is folded in edge order), else within tolerance."""
+    for name, c in golden_cases.items():
+        g = golden_graph(c)
+        for app, key, kw, iters in [(gx.APP_PAGERANK_REF, "pr", {}, 20), (gx.APP_SSSP, "sssp0", {"source": 0}, 200),
+                                    (gx.APP_CC, "cc", {}, 200)]:
+            with engine_for(g, layout=1) as e:
+                st = e.run(app, iters, **kw)
+                vals = e.values()
+                assert np.array_equal(run_changed(e, st["iterations"]), c[f"{key}_changed"]) or app == gx.APP_PAGERANK_REF
+            if app == gx.APP_PAGERANK_REF and np.diff(g.off).max() > 512:
+                assert np.abs(vals.astype(np.float64) - c[key]).max() / c[key].max() < 1e-3, name
+            else:
+                assert np.array_equal(vals.view(np.uint32), c[key].view(np.uint32)), (name, key)
+    g = gx.rmat_graph(15, 16, seed=7, P=8, weight_seed=99)
+    ref, _, _ = O.run(O.SSSP, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 1000, weights=g.weights, source=0)
+    with engine_for(g, layout=1) as e:
+        e.run(gx.APP_SSSP, 1000, source=0, weighted=True)
+        assert np.array_equal(e.values(), ref)
+        e.run(gx.APP_PAGERANK_REF, 20)
+        pr = e.values().astype(np.float64)
+    pref, _, _ = O.run(O.PAGERANK_REF, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 20)
+    assert np.abs(pr - pref).max() / pref.max() < 1e-5
+
+
 @pytest.mark.parametrize("push", [1, 0])
 @pytest.mark.parametrize("source", [1, 0])
 def test_sssp_unit_bitexact_vs_reference(golden_cases, push, source):
@@ -141,18 +168,29 @@ def test_indegree_app():
 
 
 def test_streamed_shards_match_resident():
-    """A shard-cache budget far below the graph forces the streaming ring;
-    results are bit-identical to the all-resident run."""
+    """A shard-cache budget far below the graph forces the streaming ring.
+    In exact-order mode both runs fold every list in edge order, so results
+    are bit-identical; in the default mode the resident run sums medium and
+    heavy vertices in a different (tree) order, so PageRank agrees to the
+    PageRank tolerance and SSSP/CC stay bit-identical."""
     g = gx.rmat_graph(14, 16, seed=5, P=32, weight_seed=1)
-    res = engine_for(g)
     budget = g.E * 8 // 6
-    stm = engine_for(g, cache_budget_bytes=budget, stream_slots=2)
-    for app, kw in [(gx.APP_PAGERANK_REF, {}), (gx.APP_SSSP, {"source": 0, "weighted": True}), (gx.APP_CC, {})]:
-        a = res.run(app, 30, **kw)
-        b = stm.run(app, 30, **kw)
-        assert np.array_equal(res.values().view(np.uint32), stm.values().view(np.uint32)), app
-        assert a["iterations"] == b["iterations"]
-        assert 0 < b["shards_resident"] < g.P and b["h2d_bytes"] > 0
+    for exact in (1, 0):
+        res = engine_for(g, exact_order=exact)
+        stm = engine_for(g, cache_budget_bytes=budget, stream_slots=2, exact_order=exact)
+        for app, kw in [(gx.APP_PAGERANK_REF, {}), (gx.APP_SSSP, {"source": 0, "weighted": True}),
+                        (gx.APP_CC, {})]:
+            a = res.run(app, 30, **kw)
+            b = stm.run(app, 30, **kw)
+            va, vb = res.values(), stm.values()
+            if exact or app != gx.APP_PAGERANK_REF:
+                assert np.array_equal(va.view(np.uint32), vb.view(np.uint32)), (exact, app)
+            else:
+                assert np.abs(va.astype(np.float64) - vb).max() / va.max() < 1e-6
+            assert a["iterations"] == b["iterations"]
+            assert 0 < b["shards_resident"] < g.P and b["h2d_bytes"] > 0
+        res.close()
+        stm.close()
 
 
 def test_load_shards_from_directory(tmp_path):

@@ -112,3 +112,19 @@ def test_edge_weights():
     assert not np.array_equal(w, gx.edge_weights(78, g))
     h = g.with_partitions(3)
     assert np.array_equal(gx.edge_weights(77, h), w)   # a function of (u, v), not of the layout
+
+
+def test_convert_edge_list(tmp_path):
+    src, dst = gx.rmat_edges(10, 6000, seed=12)
+    lines = ["# comment", "% another"] + [f"{a}\t{b}" for a, b in zip(src.tolist(), dst.tolist())]
+    (tmp_path / "g.tsv").write_text("\n".join(lines) + "\n")
+    E = gx.convert_edge_list(tmp_path / "g.tsv", 1024, 5, tmp_path / "s")
+    h = gx.read_shards(tmp_path / "s", 1024, 5)
+    off, col = gx.build_csc(1024, src, dst)
+    assert E == off[-1] == h.E
+    assert np.array_equal(h.off, off) and np.array_equal(h.col, col)
+    assert np.array_equal(h.bounds, gx.partition_bounds(1024, off, 5))
+    (tmp_path / "bad.tsv").write_text("1 2\n3 x\n")
+    with pytest.raises(gx.GxError) as ei:
+        gx.convert_edge_list(tmp_path / "bad.tsv", 1024, 2, tmp_path / "t")
+    assert ei.value.status == gx.GX_ERR_FORMAT
