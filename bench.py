@@ -458,6 +458,8 @@ def run_warm(args):
     for i in range(256):
         s = int(rng.integers(16, 21))
         ja, jb, jc = rng.uniform(-0.05, 0.05, size=3)
+        while 0.57 + ja + 0.19 + jb + 0.19 + jc > 0.99:   # keep d = 1 - a - b - c >= 0.01
+            ja, jb, jc = rng.uniform(-0.05, 0.05, size=3)
         g = gx.rmat_graph(s, 16, seed=SEED + 17 * i, P=16, a=0.57 + ja, b=0.19 + jb, c=0.19 + jc)
         with gx.Engine() as e:
             e.load(g)

@@ -40,6 +40,7 @@ class GxError(RuntimeError):
 
 class Config(C.Structure):
     _fields_ = [("device", C.c_int32), ("cache_budget_bytes", C.c_int64), ("stream_slots", C.c_int32),
+                ("copy_streams", C.c_int32),
                 ("selective_threshold", C.c_double), ("heavy_degree", C.c_int32), ("tile_edges", C.c_int32),
                 ("exact_order", C.c_int32),
                 ("push_sparse", C.c_int32), ("use_graph", C.c_int32), ("wait_limit", C.c_uint32),

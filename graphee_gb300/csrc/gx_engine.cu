@@ -305,7 +305,7 @@ gx_status plan_shards(gx_engine* e) {
       e->dev_base[p] = pos - lo[p];  // d_col + dev_base[p] is indexed by global edge id
       pos += hi[p] - lo[p] + 4;
     }
-    const int slots = std::max(2, e->cfg.stream_slots);
+    const int slots = std::max({2, e->cfg.stream_slots, static_cast<int>(e->s_copies.size())});
     e->slot_elems = max_stream + 8;
     for (auto ptr : e->slot_col) cudaFree(ptr);
     for (auto ptr : e->slot_w) cudaFree(ptr);
@@ -631,8 +631,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
       const Ctl& hc = *e->h_ctl;
       if (hc.done) break;
       const bool sel = hc.mode == MODE_SELECTIVE;
-      GX_CUDA(cudaEventRecord(c0, e->s_copy));
       GX_CUDA(cudaEventRecord(k0, e->s_comp));
+      GX_CUDA(cudaEventRecord(c0, e->s_comp));
       for (int32_t p = 0; p < e->P; ++p) {
         PullArgs sp = pa;
         sp.u_begin = e->unit_begin[p];
@@ -646,16 +646,17 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
         } else {
           const int64_t lo = e->off[e->bounds[p]] & ~3ll;
           const int64_t n = std::min<int64_t>((e->off[e->bounds[p + 1]] + 3) & ~3ll, e->E + 4) - lo;
-          GX_CUDA(cudaStreamWaitEvent(e->s_copy, e->slot_free[slot], 0));
-          GX_CUDA(cudaMemcpyAsync(e->slot_col[slot], e->h_col + lo, n * sizeof(int32_t), cudaMemcpyHostToDevice,
-                                  e->s_copy));
+          // Slots alternate over the copy streams, so several copy engines
+          // move shards at once.
+          cudaStream_t cs = e->s_copies[slot % e->s_copies.size()];
+          GX_CUDA(cudaStreamWaitEvent(cs, e->slot_free[slot], 0));
+          GX_CUDA(cudaMemcpyAsync(e->slot_col[slot], e->h_col + lo, n * sizeof(int32_t), cudaMemcpyHostToDevice, cs));
           h2d_bytes += n * sizeof(int32_t);
           if (weighted) {
-            GX_CUDA(cudaMemcpyAsync(e->slot_w[slot], e->h_w + lo, n * sizeof(uint32_t), cudaMemcpyHostToDevice,
-                                    e->s_copy));
+            GX_CUDA(cudaMemcpyAsync(e->slot_w[slot], e->h_w + lo, n * sizeof(uint32_t), cudaMemcpyHostToDevice, cs));
             h2d_bytes += n * sizeof(uint32_t);
           }
-          GX_CUDA(cudaEventRecord(e->slot_ready[slot], e->s_copy));
+          GX_CUDA(cudaEventRecord(e->slot_ready[slot], cs));
           GX_CUDA(cudaStreamWaitEvent(e->s_comp, e->slot_ready[slot], 0));
           sp.col = e->slot_col[slot] - lo;
           if (weighted) sp.w = e->slot_w[slot] - lo;
@@ -672,15 +673,20 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
           slot = (slot + 1) % slots;
         }
       }
-      GX_CUDA(cudaEventRecord(c1, e->s_copy));
       GX_CUDA(cudaEventRecord(k1, e->s_comp));
       finalize_kernel<APP><<<grid_fin, kThreads, 0, e->s_comp>>>(fa);
       GX_CUDA(cudaGetLastError());
       ++launches;
-      GX_CUDA(cudaStreamSynchronize(e->s_copy));
-      GX_CUDA(cudaStreamSynchronize(e->s_comp));
+      // Copy time: from the step's start to the last copy stream's end.
       float ms_c = 0, ms_k = 0;
-      cudaEventElapsedTime(&ms_c, c0, c1);
+      for (cudaStream_t cs : e->s_copies) {
+        GX_CUDA(cudaEventRecord(c1, cs));
+        GX_CUDA(cudaEventSynchronize(c1));
+        float t = 0;
+        cudaEventElapsedTime(&t, c0, c1);
+        ms_c = std::max(ms_c, t);
+      }
+      GX_CUDA(cudaStreamSynchronize(e->s_comp));
       cudaEventElapsedTime(&ms_k, k0, k1);
       copy_ms += ms_c;
       comp_ms += ms_k;
@@ -738,7 +744,8 @@ void gx_config_default(gx_config* cfg) {
   if (!cfg) return;
   cfg->device = 0;
   cfg->cache_budget_bytes = -1;
-  cfg->stream_slots = 3;
+  cfg->stream_slots = 4;
+  cfg->copy_streams = 2;
   cfg->selective_threshold = 0.001;
   cfg->heavy_degree = 4096;
   cfg->tile_edges = 2048;
@@ -782,6 +789,12 @@ gx_status gx_create(const gx_config* cfg, gx_engine** out) {
   GX_CUDA(cudaDeviceGetAttribute(&e->n_sm, cudaDevAttrMultiProcessorCount, e->dev));
   GX_CUDA(cudaStreamCreateWithFlags(&e->s_comp, cudaStreamNonBlocking));
   GX_CUDA(cudaStreamCreateWithFlags(&e->s_copy, cudaStreamNonBlocking));
+  e->s_copies.push_back(e->s_copy);
+  for (int i = 1; i < std::max(1, c.copy_streams); ++i) {
+    cudaStream_t cs;
+    GX_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    e->s_copies.push_back(cs);
+  }
   GX_TRY(alloc_ctl(e.get()));
   *out = e.release();
   return GX_OK;

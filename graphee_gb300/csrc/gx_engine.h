@@ -66,6 +66,7 @@ struct gx_engine {
   int dev = 0;
   int n_sm = 0;
   cudaStream_t s_comp = nullptr, s_copy = nullptr;
+  std::vector<cudaStream_t> s_copies;  // s_copy first
   bool loaded = false;
 
   // graph (host side)
@@ -208,7 +209,8 @@ struct gx_engine {
     if (h_ctl) cudaFreeHost(h_ctl);
     h_ctl = nullptr;
     if (s_comp) cudaStreamDestroy(s_comp);
-    if (s_copy) cudaStreamDestroy(s_copy);
+    for (cudaStream_t cs : s_copies) cudaStreamDestroy(cs);
+    s_copies.clear();
     s_comp = s_copy = nullptr;
   }
 };

@@ -221,8 +221,17 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long x) {
 // Results are deterministic run to run in both modes.
 // ---------------------------------------------------------------------------
 constexpr int kHeavyChunk = 2048;
-constexpr int kLaneMaxDegree = 32;   // longest list a lane walks alone
-constexpr int kGrab = 4;             // units a warp claims per atomic
+#ifndef GX_LANE_MAX
+#define GX_LANE_MAX 32
+#endif
+#ifndef GX_GRAB
+#define GX_GRAB 4
+#endif
+#ifndef GX_TILE_PREFETCH
+#define GX_TILE_PREFETCH 0
+#endif
+constexpr int kLaneMaxDegree = GX_LANE_MAX;  // longest list a lane walks alone
+constexpr int kGrab = GX_GRAB;               // units a warp claims per atomic
 constexpr int kQueues = 64;          // work-unit cursors per launch
 
 template <class T>
@@ -302,7 +311,7 @@ __device__ __forceinline__ typename AppTraits<APP>::T warp_reduce_range(const Pu
 }
 
 #ifndef GX_PULL_MIN_BLOCKS
-#define GX_PULL_MIN_BLOCKS 5
+#define GX_PULL_MIN_BLOCKS 4
 #endif
 
 template <int APP, bool EXACT>
@@ -358,9 +367,29 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
       myu = a.units[u0 + lane];
       if (selective) mysh = a.unit_shard[u0 + lane];
     }
+    // A tile's per-lane offsets, old value and out-degree are loaded one
+    // unit ahead, so those loads overlap the previous unit's gathers.
+    int64_t pbeg = 0, pend = 0;
+    T pold = T(0);
+    int32_t pod = 0;
+    auto prefetch_tile = [&](int j) {
+      const int px = __shfl_sync(0xffffffffu, myu.x, j), py = __shfl_sync(0xffffffffu, myu.y, j);
+      if (px >= 0 && lane < py - px) {
+        const int pv = px + lane;
+        pbeg = a.off[pv];
+        pend = a.off[pv + 1];
+        pold = __ldcs(static_cast<const T*>(src_val) + pv);
+        if constexpr (is_pr<APP>()) pod = __ldcs(a.outdeg + pv);
+      }
+    };
+    if (GX_TILE_PREFETCH) prefetch_tile(0);
     for (int j = 0; j < cnt; ++j) {
       const int2 wu = make_int2(__shfl_sync(0xffffffffu, myu.x, j), __shfl_sync(0xffffffffu, myu.y, j));
       const bool on = !selective || ((smask >> (__shfl_sync(0xffffffffu, mysh, j) / group)) & 1ull);
+      const int64_t cbeg = pbeg, cend = pend;
+      const T cold = pold;
+      const int32_t cod = pod;
+      if (GX_TILE_PREFETCH && j + 1 < cnt) prefetch_tile(j + 1);
       if (wu.x < 0) {
         // ---- heavy chunk ----
         const int h = -wu.x - 1;
@@ -413,16 +442,21 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
       int64_t beg = 0, end = 0;
       T old = T(0);
       int32_t od = 0;
-      if (lane < n) {
+      if (GX_TILE_PREFETCH) {
+        if (lane < n) {
+          beg = cbeg;
+          end = cend;
+          old = cold;
+          od = cod;
+        }
+      } else if (lane < n) {
         beg = a.off[v];
         end = a.off[v + 1];
-      }
-      // Vertices above the heavy threshold are applied by their own units.
-      const bool valid = lane < n && end - beg <= a.heavy_deg;
-      if (valid) {
         old = __ldcs(static_cast<const T*>(src_val) + v);
         if constexpr (is_pr<APP>()) od = __ldcs(a.outdeg + v);
       }
+      // Vertices above the heavy threshold are applied by their own units.
+      const bool valid = lane < n && end - beg <= a.heavy_deg;
       if (!on) {
         if (valid) {
           static_cast<T*>(dst_val)[v] = old;

@@ -70,11 +70,26 @@ __global__ void mlp_nbr_kernel(const int64_t* off, const int32_t* outdeg, int32_
   }
 }
 
+// Accumulators of one vertex's feature pass.
+struct FeatAcc {
+  float sum_g = 0.f, max_g = 0.f, sum_inv = 0.f;
+  long long sum_in = 0;
+  __device__ __forceinline__ void add(const NbrInfo& x) {
+    sum_g += x.log_out;
+    max_g = fmaxf(max_g, x.log_out);
+    sum_in += x.indeg;
+    sum_inv += x.inv_out;
+  }
+};
+
 // Features, plus each CTA's share of the uniform start's first-step L1
-// residual sum |r1 - 1/N| (standard PageRank).
-__global__ void mlp_features_kernel(const int64_t* off, const int32_t* col, const int32_t* outdeg,
-                                    const NbrInfo* nb, int32_t V, double damping, double dangling0,
-                                    float* feat, double* part_resid) {
+// residual sum |r1 - 1/N| (standard PageRank).  Tiles of 32 consecutive
+// vertices: a lane walks a list of up to 64 edges with 128-bit index loads
+// and 8 gathers in flight; longer lists are swept by the whole warp.
+__global__ void __launch_bounds__(256, 3) mlp_features_kernel(const int64_t* off, const int32_t* col,
+                                                           const int32_t* outdeg, const NbrInfo* nb, int32_t V,
+                                                           double damping, double dangling0, float* feat,
+                                                           double* part_resid) {
   __shared__ double s_red[8];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int warps = gridDim.x * (blockDim.x >> 5);
@@ -88,57 +103,51 @@ __global__ void mlp_features_kernel(const int64_t* off, const int32_t* col, cons
       beg = off[v];
       end = off[v + 1];
     }
-    float sum_g = 0.f, max_g = 0.f, sum_inv = 0.f;
-    double sum_in = 0;
+    FeatAcc f;
     const bool longl = valid && end - beg > 64;
     if (valid && !longl) {
-      for (int64_t k = beg; k < end; ++k) {
-        const NbrInfo x = nb[col[k]];
-        sum_g += x.log_out;
-        max_g = fmaxf(max_g, x.log_out);
-        sum_in += x.indeg;
-        sum_inv += x.inv_out;
+      for (int64_t k = beg & ~3ll; k < end; k += 8) {
+        const int4 c0 = *reinterpret_cast<const int4*>(col + k);
+        const int4 c1 = k + 4 < end ? *reinterpret_cast<const int4*>(col + k + 4) : make_int4(0, 0, 0, 0);
+        const int cs[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+        NbrInfo x[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (k + j >= beg && k + j < end) x[j] = nb[cs[j]];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (k + j >= beg && k + j < end) f.add(x[j]);
       }
     }
     for (unsigned m = __ballot_sync(0xffffffffu, longl); m; m &= m - 1) {
       const int l = __ffs(m) - 1;
       const int64_t bl = __shfl_sync(0xffffffffu, beg, l), el = __shfl_sync(0xffffffffu, end, l);
-      float sg = 0.f, mg = 0.f, si = 0.f;
-      double sn = 0;
-      for (int64_t k = bl + lane; k < el; k += 32) {
-        const NbrInfo x = nb[col[k]];
-        sg += x.log_out;
-        mg = fmaxf(mg, x.log_out);
-        sn += x.indeg;
-        si += x.inv_out;
+      FeatAcc g;
+      for (int64_t k0 = bl + lane; k0 < el; k0 += 256) {
+        NbrInfo x[8];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (k0 + 32 * j < el) x[j] = nb[col[k0 + 32 * j]];
+#pragma unroll
+        for (int j = 0; j < 8; ++j)
+          if (k0 + 32 * j < el) g.add(x[j]);
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
-        sg += __shfl_xor_sync(0xffffffffu, sg, o);
-        mg = fmaxf(mg, __shfl_xor_sync(0xffffffffu, mg, o));
-        sn += __shfl_xor_sync(0xffffffffu, sn, o);
-        si += __shfl_xor_sync(0xffffffffu, si, o);
+        g.sum_g += __shfl_xor_sync(0xffffffffu, g.sum_g, o);
+        g.max_g = fmaxf(g.max_g, __shfl_xor_sync(0xffffffffu, g.max_g, o));
+        g.sum_in += __shfl_xor_sync(0xffffffffu, g.sum_in, o);
+        g.sum_inv += __shfl_xor_sync(0xffffffffu, g.sum_inv, o);
       }
-      if (lane == l) {
-        sum_g = sg;
-        max_g = mg;
-        sum_in = sn;
-        sum_inv = si;
-      }
+      if (lane == l) f = g;
     }
     if (valid) {
-      const double deg = static_cast<double>(end - beg);
+      const float deg = static_cast<float>(end - beg);
       const int32_t od = outdeg[v];
-      float* f = feat + static_cast<size_t>(v) * kFeatStride;
-      f[0] = log1pf(static_cast<float>(deg));
-      f[1] = log1pf(static_cast<float>(od));
-      f[2] = deg > 0 ? sum_g / static_cast<float>(deg) : 0.f;
-      f[3] = max_g;
-      f[4] = static_cast<float>(log1p(sum_in));
-      f[5] = od == 0 ? 1.f : 0.f;
-      f[6] = 0.f;
-      f[7] = 0.f;
-      const double r1 = (1.0 - damping) * invn + damping * (sum_inv * invn + dangling0 * invn);
+      float4* fo = reinterpret_cast<float4*>(feat + static_cast<size_t>(v) * kFeatStride);
+      fo[0] = make_float4(log1pf(deg), log1pf(static_cast<float>(od)), deg > 0 ? f.sum_g / deg : 0.f, f.max_g);
+      fo[1] = make_float4(static_cast<float>(log1p(static_cast<double>(f.sum_in))), od == 0 ? 1.f : 0.f, 0.f, 0.f);
+      const double r1 = (1.0 - damping) * invn + damping * (f.sum_inv * invn + dangling0 * invn);
       resid += fabs(r1 - invn);
     }
   }
@@ -566,7 +575,7 @@ gx_status engine_features(gx_engine* e, double damping, float* feat, double* uni
   NbrInfo* nb = nullptr;
   double* part = nullptr;
   GX_TRY(dev_alloc(&nb, static_cast<size_t>(V)));
-  const int grid = e->n_sm * 8;
+  const int grid = e->n_sm * 16;
   gx_status st = dev_alloc(&part, static_cast<size_t>(grid));
   if (st != GX_OK) {
     cudaFree(nb);

@@ -62,7 +62,8 @@ typedef struct gx_config {
   int32_t device;              /* CUDA device ordinal (default 0) */
   int64_t cache_budget_bytes;  /* HBM shard-cache budget for edge data; <0 = unlimited.
                                   Replaces EDGE_CACHE_SIZE (GraphMP/system/Global.h:52). */
-  int32_t stream_slots;        /* device slots in the streaming ring (>=2, default 3) */
+  int32_t stream_slots;        /* device slots in the streaming ring (>=2, default 4) */
+  int32_t copy_streams;        /* H2D copy streams the slots alternate over (default 2) */
   double selective_threshold;  /* BF_THRE (GraphMP/system/Global.h:57), default 0.001 */
   int32_t heavy_degree;        /* in-degree above which a vertex gets its own warp units, split
                                   into 2048-edge chunks (default 4096, minimum 32) */
