@@ -745,7 +745,7 @@ void gx_config_default(gx_config* cfg) {
   cfg->device = 0;
   cfg->cache_budget_bytes = -1;
   cfg->stream_slots = 4;
-  cfg->copy_streams = 2;
+  cfg->copy_streams = 1;
   cfg->selective_threshold = 0.001;
   cfg->heavy_degree = 4096;
   cfg->tile_edges = 2048;
@@ -833,6 +833,8 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
     gx_status st = gx_out_degree(V, off, col, e->outdeg.data());
     if (st != GX_OK) return st;
   }
+  e->n_dangling = 0;
+  for (int32_t v = 0; v < V; ++v) e->n_dangling += e->outdeg[v] == 0;
   // Validate source ids once on the host (the kernels index vertex arrays with them).
   int bad = 0;
 #pragma omp parallel for reduction(| : bad)

@@ -75,6 +75,7 @@ struct gx_engine {
   std::vector<int32_t> bounds;
   std::vector<int64_t> off;
   std::vector<int32_t> outdeg;
+  int64_t n_dangling = 0;            // vertices of out-degree 0
   std::vector<int2> units;
   std::vector<int32_t> unit_shard;
   std::vector<int32_t> unit_begin;  // P+1

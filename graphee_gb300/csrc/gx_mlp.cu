@@ -1,4 +1,4 @@
-// Learned PageRank warm start: a 6 -> 64 -> 64 -> 1 MLP (GELU hidden
+// Learned PageRank warm start: a 6 -> 64 -> 64 -> 1 MLP (GELU, tanh form, hidden
 // layers, softplus output normalised to sum 1) predicts initial ranks from
 // per-vertex degree features; standard PageRank (GX_APP_PAGERANK_STD) then
 // runs from that start to the L1 residual tolerance, and falls back to the
@@ -44,9 +44,24 @@ constexpr int kTrainSamples = 128;   // samples per training CTA
 constexpr int kTrainThreads = 256;
 constexpr int kPartStride = kNumParams + 3;  // gradient partial + loss
 
-__device__ __forceinline__ float gelu(float x) { return 0.5f * x * (1.f + erff(x * 0.70710678118654752f)); }
+// GELU in its tanh form, 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))):
+// training uses tanhf, inference the hardware tanh.approx.f32.
+constexpr float kGeluC = 0.7978845608028654f;  // sqrt(2/pi)
+constexpr float kGeluA = 0.044715f;
+__device__ __forceinline__ float gelu(float x) {
+  return 0.5f * x * (1.f + tanhf(kGeluC * (x + kGeluA * x * x * x)));
+}
 __device__ __forceinline__ float gelu_grad(float x) {
-  return 0.5f * (1.f + erff(x * 0.70710678118654752f)) + x * 0.39894228040143268f * expf(-0.5f * x * x);
+  const float t = tanhf(kGeluC * (x + kGeluA * x * x * x));
+  return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * kGeluC * (1.f + 3.f * kGeluA * x * x);
+}
+__device__ __forceinline__ float tanh_fast(float x) {
+  float y;
+  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float gelu_fast(float x) {
+  return 0.5f * x * (1.f + tanh_fast(kGeluC * (x + kGeluA * x * x * x)));
 }
 __device__ __forceinline__ float softplus(float z) { return z > 20.f ? z : log1pf(expf(z)); }
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
@@ -231,10 +246,10 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const float* feat, const
       const uint32_t b1 = *reinterpret_cast<const uint32_t*>(&sW1[8 * j + g][2 * t + 8]);
       mma_bf16(h1[j], a1, b0, b1);
       const float bl = sb1[8 * j + 2 * t], bh = sb1[8 * j + 2 * t + 1];
-      h1[j][0] = gelu(h1[j][0] + bl);
-      h1[j][1] = gelu(h1[j][1] + bh);
-      h1[j][2] = gelu(h1[j][2] + bl);
-      h1[j][3] = gelu(h1[j][3] + bh);
+      h1[j][0] = gelu_fast(h1[j][0] + bl);
+      h1[j][1] = gelu_fast(h1[j][1] + bh);
+      h1[j][2] = gelu_fast(h1[j][2] + bl);
+      h1[j][3] = gelu_fast(h1[j][3] + bh);
     }
     uint32_t a2[4][4];
 #pragma unroll
@@ -255,8 +270,8 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const float* feat, const
         mma_bf16(c, a2[kk], b0, b1);
       }
       const int n0 = 8 * j + 2 * t;
-      z0 += gelu(c[0] + sb2[n0]) * sw3[n0] + gelu(c[1] + sb2[n0 + 1]) * sw3[n0 + 1];
-      z1 += gelu(c[2] + sb2[n0]) * sw3[n0] + gelu(c[3] + sb2[n0 + 1]) * sw3[n0 + 1];
+      z0 += gelu_fast(c[0] + sb2[n0]) * sw3[n0] + gelu_fast(c[1] + sb2[n0 + 1]) * sw3[n0 + 1];
+      z1 += gelu_fast(c[2] + sb2[n0]) * sw3[n0] + gelu_fast(c[3] + sb2[n0 + 1]) * sw3[n0 + 1];
     }
     z0 += __shfl_xor_sync(0xffffffffu, z0, 1);
     z0 += __shfl_xor_sync(0xffffffffu, z0, 2);
@@ -568,30 +583,35 @@ gx_status compute_norm(gx_mlp* m) {
   return GX_OK;
 }
 
-// Features of the engine's graph into feat[V][8]; returns the uniform
-// start's first-step L1 residual.
-gx_status engine_features(gx_engine* e, double damping, float* feat, double* uniform_resid, cudaStream_t s) {
-  const int32_t V = e->V;
+// Scratch of one feature pass, allocated before any timed region.
+struct FeatScratch {
   NbrInfo* nb = nullptr;
   double* part = nullptr;
-  GX_TRY(dev_alloc(&nb, static_cast<size_t>(V)));
-  const int grid = e->n_sm * 16;
-  gx_status st = dev_alloc(&part, static_cast<size_t>(grid));
-  if (st != GX_OK) {
-    cudaFree(nb);
-    return st;
+  int grid = 0;
+  ~FeatScratch() {
+    dev_free(&nb);
+    dev_free(&part);
   }
-  int64_t n_dang = 0;
-  for (int32_t v = 0; v < V; ++v) n_dang += e->outdeg[v] == 0;
-  const double dangling0 = static_cast<double>(n_dang) / V;
-  mlp_nbr_kernel<<<grid, 256, 0, s>>>(e->d_off, e->d_outdeg, V, nb);
-  mlp_features_kernel<<<grid, 256, 0, s>>>(e->d_off, e->d_col, e->d_outdeg, nb, V, damping, dangling0, feat, part);
-  std::vector<double> h(grid);
-  cudaError_t err = cudaMemcpyAsync(h.data(), part, sizeof(double) * grid, cudaMemcpyDeviceToHost, s);
-  if (err == cudaSuccess) err = cudaStreamSynchronize(s);
-  cudaFree(nb);
-  cudaFree(part);
-  if (err != cudaSuccess) return fail(GX_ERR_CUDA, "mlp features: %s", cudaGetErrorString(err));
+  gx_status alloc(const gx_engine* e) {
+    grid = e->n_sm * 16;
+    GX_TRY(dev_alloc(&nb, static_cast<size_t>(e->V)));
+    GX_TRY(dev_alloc(&part, static_cast<size_t>(grid)));
+    return GX_OK;
+  }
+};
+
+// Features of the engine's graph into feat[V][8]; returns the uniform
+// start's first-step L1 residual.
+gx_status engine_features(gx_engine* e, double damping, float* feat, double* uniform_resid, cudaStream_t s,
+                          FeatScratch& fs) {
+  const int32_t V = e->V;
+  const double dangling0 = static_cast<double>(e->n_dangling) / V;
+  mlp_nbr_kernel<<<fs.grid, 256, 0, s>>>(e->d_off, e->d_outdeg, V, fs.nb);
+  mlp_features_kernel<<<fs.grid, 256, 0, s>>>(e->d_off, e->d_col, e->d_outdeg, fs.nb, V, damping, dangling0, feat,
+                                               fs.part);
+  std::vector<double> h(fs.grid);
+  GX_CUDA(cudaMemcpyAsync(h.data(), fs.part, sizeof(double) * fs.grid, cudaMemcpyDeviceToHost, s));
+  GX_CUDA(cudaStreamSynchronize(s));
   double r = 0;
   for (double x : h) r += x;
   if (uniform_resid) *uniform_resid = r;
@@ -692,7 +712,9 @@ gx_status gx_mlp_add_graph(gx_mlp* m, gx_engine* e, int32_t max_samples, int32_t
   float* feat = nullptr;
   GX_TRY(dev_alloc(&feat, static_cast<size_t>(V) * kFeatStride));
   std::unique_ptr<float, void (*)(float*)> fg(feat, [](float* q) { cudaFree(q); });
-  GX_TRY(engine_features(e, p.damping, feat, nullptr, m->s));
+  FeatScratch fs;
+  GX_TRY(fs.alloc(e));
+  GX_TRY(engine_features(e, p.damping, feat, nullptr, m->s, fs));
   const int64_t take = std::min<int64_t>(max_samples, V);
   const int64_t stride = V / take;
   if (m->n + take > m->cap) {
@@ -805,18 +827,20 @@ gx_status gx_mlp_predict(gx_mlp* m, gx_engine* e, double damping, float* host_ou
   std::unique_ptr<float, void (*)(float*)> fg(feat, [](float* q) { cudaFree(q); });
   GX_TRY(dev_alloc(&sv, static_cast<size_t>(V)));
   std::unique_ptr<float, void (*)(float*)> sg(sv, [](float* q) { cudaFree(q); });
-  cudaEvent_t ev[3];
-  for (auto& x : ev) GX_CUDA(cudaEventCreate(&x));
-  GX_CUDA(cudaEventRecord(ev[0], s));
-  double ures = 0;
-  GX_TRY(engine_features(e, damping, feat, &ures, s));
-  GX_CUDA(cudaEventRecord(ev[1], s));
+  FeatScratch fs;
+  GX_TRY(fs.alloc(e));
   const int grid = e->n_sm * 8;
   double *ps = nullptr, *pd = nullptr;
   GX_TRY(dev_alloc(&ps, static_cast<size_t>(grid)));
   std::unique_ptr<double, void (*)(double*)> psg(ps, [](double* q) { cudaFree(q); });
   GX_TRY(dev_alloc(&pd, static_cast<size_t>(grid)));
   std::unique_ptr<double, void (*)(double*)> pdg(pd, [](double* q) { cudaFree(q); });
+  cudaEvent_t ev[3];
+  for (auto& x : ev) GX_CUDA(cudaEventCreate(&x));
+  GX_CUDA(cudaEventRecord(ev[0], s));
+  double ures = 0;
+  GX_TRY(engine_features(e, damping, feat, &ures, s, fs));
+  GX_CUDA(cudaEventRecord(ev[1], s));
   mlp_infer_kernel<<<grid, 128, 0, s>>>(feat, m->norm, m->params, V, sv, ps, pd);
   std::vector<double> hs(grid), hd(grid);
   GX_CUDA(cudaMemcpyAsync(hs.data(), ps, sizeof(double) * grid, cudaMemcpyDeviceToHost, s));

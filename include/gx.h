@@ -63,7 +63,7 @@ typedef struct gx_config {
   int64_t cache_budget_bytes;  /* HBM shard-cache budget for edge data; <0 = unlimited.
                                   Replaces EDGE_CACHE_SIZE (GraphMP/system/Global.h:52). */
   int32_t stream_slots;        /* device slots in the streaming ring (>=2, default 4) */
-  int32_t copy_streams;        /* H2D copy streams the slots alternate over (default 2) */
+  int32_t copy_streams;        /* H2D copy streams the slots alternate over (default 1) */
   double selective_threshold;  /* BF_THRE (GraphMP/system/Global.h:57), default 0.001 */
   int32_t heavy_degree;        /* in-degree above which a vertex gets its own warp units, split
                                   into 2048-edge chunks (default 4096, minimum 32) */
@@ -205,7 +205,7 @@ gx_status gx_batch_autotune(gx_engine* e, int32_t n_inst, const int32_t* inst_vb
                             double* best_ms);
 
 /* ---- learned PageRank warm start (no reference counterpart) ----
- * MLP 6 -> 64 -> 64 -> 1 (GELU, softplus output normalised to sum 1) over
+ * MLP 6 -> 64 -> 64 -> 1 (GELU in tanh form, softplus output normalised to sum 1) over
  * per-vertex degree features: log1p(indeg), log1p(outdeg), mean and max of
  * in-neighbours' log1p(outdeg), log1p(2-hop in-degree sum), dangling flag.
  * BF16 weights, FP32 accumulation; inference on the tensor cores. */

@@ -7,7 +7,6 @@ W1[64][6], b1[64], W2[64][64], b2[64], w3[64], b3; forward uses W1, W2, w3
 rounded to BF16 (round to nearest even), biases in full precision.
 """
 import numpy as np
-from scipy.special import erf
 
 H, F = 64, 6
 
@@ -30,12 +29,17 @@ def unpack(p):
     return W1, b1, W2, b2, w3, b3
 
 
+C_GELU = np.sqrt(2 / np.pi)
+
+
 def gelu(x):
-    return 0.5 * x * (1 + erf(x / np.sqrt(2)))
+    """GELU in its tanh form, as the library computes it."""
+    return 0.5 * x * (1 + np.tanh(C_GELU * (x + 0.044715 * x ** 3)))
 
 
 def gelu_grad(x):
-    return 0.5 * (1 + erf(x / np.sqrt(2))) + x * np.exp(-0.5 * x * x) / np.sqrt(2 * np.pi)
+    t = np.tanh(C_GELU * (x + 0.044715 * x ** 3))
+    return 0.5 * (1 + t) + 0.5 * x * (1 - t * t) * C_GELU * (1 + 3 * 0.044715 * x * x)
 
 
 def softplus(z):
