@@ -5,7 +5,7 @@
 // uniform start when the warm start's first-step residual is worse than the
 // uniform start's.  No reference counterpart.
 //
-// Features of v (one pull pass over in-edges, 16-byte gather per edge):
+// Features of v (one pull pass over in-edges, 8-byte gather per edge):
 //   log1p(indeg v), log1p(outdeg v), mean and max over in-neighbours u of
 //   log1p(outdeg u), log1p(sum over in-neighbours of indeg u), [outdeg v == 0].
 // The same pass accumulates sum 1/outdeg(u), which gives the uniform start's
@@ -21,6 +21,7 @@
 // hand-written FP32 forward/backward kernels whose per-CTA weight gradients
 // are summed in CTA order, so training is deterministic.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -66,71 +67,85 @@ __device__ __forceinline__ float gelu_fast(float x) {
 __device__ __forceinline__ float softplus(float z) { return z > 20.f ? z : log1pf(expf(z)); }
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
 
-struct NbrInfo {
-  float log_out;   // log1p(outdeg)
-  int32_t indeg;
-  float inv_out;   // 1 / max(outdeg, 1)
-  int32_t pad;
+// Per-vertex data gathered once per in-edge by the feature pass (8 bytes):
+// log1p(outdeg) and 1/max(outdeg,1) as halves (finer than the BF16 the
+// network sees), in-degree as a float (exact below 2^24).
+struct __align__(8) NbrInfo {
+  __half2 lo_inv;
+  float indeg;
 };
 
 __global__ void mlp_nbr_kernel(const int64_t* off, const int32_t* outdeg, int32_t V, NbrInfo* nb) {
   for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
     const int32_t od = outdeg[v];
     NbrInfo x;
-    x.log_out = log1pf(static_cast<float>(od));
-    x.indeg = static_cast<int32_t>(off[v + 1] - off[v]);
-    x.inv_out = 1.f / static_cast<float>(od > 0 ? od : 1);
-    x.pad = 0;
+    x.lo_inv = __floats2half2_rn(log1pf(static_cast<float>(od)), 1.f / static_cast<float>(od > 0 ? od : 1));
+    x.indeg = static_cast<float>(off[v + 1] - off[v]);
     nb[v] = x;
   }
 }
 
 // Accumulators of one vertex's feature pass.
 struct FeatAcc {
-  float sum_g = 0.f, max_g = 0.f, sum_inv = 0.f;
-  long long sum_in = 0;
+  float sum_g = 0.f, max_g = 0.f, sum_inv = 0.f, sum_in = 0.f;
   __device__ __forceinline__ void add(const NbrInfo& x) {
-    sum_g += x.log_out;
-    max_g = fmaxf(max_g, x.log_out);
+    const float2 li = __half22float2(x.lo_inv);
+    sum_g += li.x;
+    max_g = fmaxf(max_g, li.x);
     sum_in += x.indeg;
-    sum_inv += x.inv_out;
+    sum_inv += li.y;
   }
 };
 
 // Features, plus each CTA's share of the uniform start's first-step L1
 // residual sum |r1 - 1/N| (standard PageRank).  Tiles of 32 consecutive
-// vertices: a lane walks a list of up to 64 edges with 128-bit index loads
-// and 8 gathers in flight; longer lists are swept by the whole warp.
+// vertices: a lane walks a list of up to 32 edges with 128-bit index loads
+// (the next one prefetched) and 4 gathers in flight; longer lists are swept
+// by the whole warp.
 __global__ void __launch_bounds__(256, 3) mlp_features_kernel(const int64_t* off, const int32_t* col,
                                                            const int32_t* outdeg, const NbrInfo* nb, int32_t V,
-                                                           double damping, double dangling0, float* feat,
-                                                           double* part_resid) {
+                                                           const int2* units, int32_t n_units, unsigned int* cursor,
+                                                           int64_t heavy_deg, double damping, double dangling0,
+                                                           float* feat, double* part_resid) {
   __shared__ double s_red[8];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int warps = gridDim.x * (blockDim.x >> 5);
   const double invn = 1.0 / V;
   double resid = 0;
-  for (int t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; t * 32 < V; t += warps) {
-    const int v = t * 32 + lane;
-    const bool valid = v < V;
+  // The engine's work units (edge-capped tiles of consecutive vertices),
+  // claimed dynamically; heavy chunks belong to mlp_heavy_features_kernel.
+  for (int u = 0;; ++u) {
+    if ((u & 3) == 0) {  // claim four units per atomic
+      int c = 0;
+      if (lane == 0) c = static_cast<int>(atomicAdd(cursor, 4u));
+      u = __shfl_sync(0xffffffffu, c, 0);
+    }
+    if (u >= n_units) break;
+    const int2 wu = units[u];
+    if (wu.x < 0) continue;
+    const int v = wu.x + lane;
+    const bool valid = v < wu.y;
     int64_t beg = 0, end = 0;
     if (valid) {
       beg = off[v];
       end = off[v + 1];
     }
+    // Lists above heavy_deg belong to mlp_heavy_features_kernel.
+    const bool mine = valid && end - beg <= heavy_deg;
     FeatAcc f;
-    const bool longl = valid && end - beg > 64;
-    if (valid && !longl) {
-      for (int64_t k = beg & ~3ll; k < end; k += 8) {
-        const int4 c0 = *reinterpret_cast<const int4*>(col + k);
-        const int4 c1 = k + 4 < end ? *reinterpret_cast<const int4*>(col + k + 4) : make_int4(0, 0, 0, 0);
-        const int cs[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
-        NbrInfo x[8];
+    const bool longl = mine && end - beg > 32;
+    if (mine && !longl) {
+      int64_t k = beg & ~3ll;
+      int4 c0 = make_int4(0, 0, 0, 0);
+      if (k < end) c0 = *reinterpret_cast<const int4*>(col + k);
+      for (; k < end; k += 4) {
+        const int cs[4] = {c0.x, c0.y, c0.z, c0.w};
+        if (k + 4 < end) c0 = *reinterpret_cast<const int4*>(col + k + 4);  // next step's indices
+        NbrInfo x[4];
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+        for (int j = 0; j < 4; ++j)
           if (k + j >= beg && k + j < end) x[j] = nb[cs[j]];
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+        for (int j = 0; j < 4; ++j)
           if (k + j >= beg && k + j < end) f.add(x[j]);
       }
     }
@@ -138,13 +153,13 @@ __global__ void __launch_bounds__(256, 3) mlp_features_kernel(const int64_t* off
       const int l = __ffs(m) - 1;
       const int64_t bl = __shfl_sync(0xffffffffu, beg, l), el = __shfl_sync(0xffffffffu, end, l);
       FeatAcc g;
-      for (int64_t k0 = bl + lane; k0 < el; k0 += 256) {
-        NbrInfo x[8];
+      for (int64_t k0 = bl + lane; k0 < el; k0 += 128) {
+        NbrInfo x[4];
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+        for (int j = 0; j < 4; ++j)
           if (k0 + 32 * j < el) x[j] = nb[col[k0 + 32 * j]];
 #pragma unroll
-        for (int j = 0; j < 8; ++j)
+        for (int j = 0; j < 4; ++j)
           if (k0 + 32 * j < el) g.add(x[j]);
       }
 #pragma unroll
@@ -156,7 +171,7 @@ __global__ void __launch_bounds__(256, 3) mlp_features_kernel(const int64_t* off
       }
       if (lane == l) f = g;
     }
-    if (valid) {
+    if (mine) {
       const float deg = static_cast<float>(end - beg);
       const int32_t od = outdeg[v];
       float4* fo = reinterpret_cast<float4*>(feat + static_cast<size_t>(v) * kFeatStride);
@@ -174,6 +189,64 @@ __global__ void __launch_bounds__(256, 3) mlp_features_kernel(const int64_t* off
     double t = 0;
     for (int i = 0; i < (blockDim.x >> 5); ++i) t += s_red[i];
     part_resid[blockIdx.x] = t;
+  }
+}
+
+// Features of the vertices above the heavy threshold: a CTA per vertex,
+// per-thread partials combined in a fixed order; writes the vertex's share
+// of the uniform first-step residual to part_resid[i].
+__global__ void __launch_bounds__(256) mlp_heavy_features_kernel(const int64_t* off, const int32_t* col,
+                                                                 const int32_t* outdeg, const NbrInfo* nb,
+                                                                 const int4* heavy, int32_t n_heavy, int32_t V,
+                                                                 double damping, double dangling0, float* feat,
+                                                                 double* part_resid) {
+  __shared__ float s_g[8], s_m[8], s_i[8], s_n[8];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int i = blockIdx.x; i < n_heavy; i += gridDim.x) {
+    const int v = heavy[i].x;
+    const int64_t beg = off[v], end = off[v + 1];
+    FeatAcc g;
+    for (int64_t k0 = beg + threadIdx.x; k0 < end; k0 += 4 * 256) {
+      NbrInfo x[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (k0 + 256 * j < end) x[j] = nb[col[k0 + 256 * j]];
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+        if (k0 + 256 * j < end) g.add(x[j]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      g.sum_g += __shfl_xor_sync(0xffffffffu, g.sum_g, o);
+      g.max_g = fmaxf(g.max_g, __shfl_xor_sync(0xffffffffu, g.max_g, o));
+      g.sum_in += __shfl_xor_sync(0xffffffffu, g.sum_in, o);
+      g.sum_inv += __shfl_xor_sync(0xffffffffu, g.sum_inv, o);
+    }
+    if (lane == 0) {
+      s_g[wid] = g.sum_g;
+      s_m[wid] = g.max_g;
+      s_i[wid] = g.sum_inv;
+      s_n[wid] = g.sum_in;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      FeatAcc f;
+      for (int w = 0; w < 8; ++w) {
+        f.sum_g += s_g[w];
+        f.max_g = fmaxf(f.max_g, s_m[w]);
+        f.sum_inv += s_i[w];
+        f.sum_in += s_n[w];
+      }
+      const float deg = static_cast<float>(end - beg);
+      const int32_t od = outdeg[v];
+      float4* fo = reinterpret_cast<float4*>(feat + static_cast<size_t>(v) * kFeatStride);
+      fo[0] = make_float4(log1pf(deg), log1pf(static_cast<float>(od)), deg > 0 ? f.sum_g / deg : 0.f, f.max_g);
+      fo[1] = make_float4(static_cast<float>(log1p(static_cast<double>(f.sum_in))), od == 0 ? 1.f : 0.f, 0.f, 0.f);
+      const double invn = 1.0 / V;
+      const double r1 = (1.0 - damping) * invn + damping * (f.sum_inv * invn + dangling0 * invn);
+      part_resid[i] = fabs(r1 - invn);
+    }
+    __syncthreads();
   }
 }
 
@@ -587,15 +660,20 @@ gx_status compute_norm(gx_mlp* m) {
 struct FeatScratch {
   NbrInfo* nb = nullptr;
   double* part = nullptr;
+  unsigned int* cursor = nullptr;
   int grid = 0;
   ~FeatScratch() {
     dev_free(&nb);
     dev_free(&part);
+    dev_free(&cursor);
   }
   gx_status alloc(const gx_engine* e) {
-    grid = e->n_sm * 16;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mlp_features_kernel, 256, 0);
+    grid = std::max(1, per_sm) * e->n_sm;
     GX_TRY(dev_alloc(&nb, static_cast<size_t>(e->V)));
-    GX_TRY(dev_alloc(&part, static_cast<size_t>(grid)));
+    GX_TRY(dev_alloc(&part, static_cast<size_t>(grid) + e->heavy.size()));
+    GX_TRY(dev_alloc(&cursor, 1));
     return GX_OK;
   }
 };
@@ -606,11 +684,22 @@ gx_status engine_features(gx_engine* e, double damping, float* feat, double* uni
                           FeatScratch& fs) {
   const int32_t V = e->V;
   const double dangling0 = static_cast<double>(e->n_dangling) / V;
+  // The engine's heavy-vertex table (in-degree above heavy_degree) marks
+  // the lists the tile kernel leaves to a CTA each.
+  const int32_t n_heavy = static_cast<int32_t>(e->heavy.size());
+  const int64_t heavy_deg = e->cfg.exact_order ? INT64_MAX : std::max(e->cfg.heavy_degree, 32);
   mlp_nbr_kernel<<<fs.grid, 256, 0, s>>>(e->d_off, e->d_outdeg, V, fs.nb);
-  mlp_features_kernel<<<fs.grid, 256, 0, s>>>(e->d_off, e->d_col, e->d_outdeg, fs.nb, V, damping, dangling0, feat,
-                                               fs.part);
-  std::vector<double> h(fs.grid);
-  GX_CUDA(cudaMemcpyAsync(h.data(), fs.part, sizeof(double) * fs.grid, cudaMemcpyDeviceToHost, s));
+  GX_CUDA(cudaMemsetAsync(fs.cursor, 0, sizeof(unsigned int), s));
+  GX_CUDA(cudaMemsetAsync(fs.part, 0, sizeof(double) * fs.grid, s));
+  mlp_features_kernel<<<fs.grid, 256, 0, s>>>(e->d_off, e->d_col, e->d_outdeg, fs.nb, V, e->d_units,
+                                               static_cast<int32_t>(e->units.size()), fs.cursor,
+                                               n_heavy ? heavy_deg : INT64_MAX, damping, dangling0, feat, fs.part);
+  if (n_heavy)
+    mlp_heavy_features_kernel<<<std::min(n_heavy, e->n_sm * 8), 256, 0, s>>>(
+        e->d_off, e->d_col, e->d_outdeg, fs.nb, e->d_heavy, n_heavy, V, damping, dangling0, feat, fs.part + fs.grid);
+  GX_CUDA(cudaGetLastError());
+  std::vector<double> h(static_cast<size_t>(fs.grid) + n_heavy);
+  GX_CUDA(cudaMemcpyAsync(h.data(), fs.part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s));
   GX_CUDA(cudaStreamSynchronize(s));
   double r = 0;
   for (double x : h) r += x;
