@@ -13,7 +13,8 @@
 //
 // Training target: t_v = log(N * r_v) of converged standard PageRank; the
 // network's per-vertex output y_v = log softplus(z_v) is fitted to t_v in
-// squared error, so the normalised softplus output approximates r.
+// squared error weighted by min(N * r_v, 100), so the normalised softplus
+// output approximates r where the L1 error lives.
 // Weights: FP32 master copy updated by Adam; every forward pass (training
 // and inference) uses the weights rounded to BF16, with FP32 accumulation.
 // Inference runs on the tensor cores (mma.sync m16n8k16 BF16, the layer-1
@@ -44,6 +45,7 @@ constexpr int kFeatStride = 8;
 constexpr int kTrainSamples = 128;   // samples per training CTA
 constexpr int kTrainThreads = 256;
 constexpr int kPartStride = kNumParams + 3;  // gradient partial + loss
+constexpr float kLossWeightCap = 100.f;
 
 // GELU in its tanh form, 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))):
 // training uses tanhf, inference the hardware tanh.approx.f32.
@@ -464,9 +466,12 @@ __global__ void __launch_bounds__(kTrainThreads) mlp_train_kernel(const float* x
     const float sp = softplus(z);
     const float y = logf(sp);
     const float e = live ? y - Tg[s] : 0.f;
-    loss += e * e;
+    // Weight N*r_v = exp(t): the L1 error of the start vector is carried by
+    // the high-rank vertices (capped so single hubs do not dominate).
+    const float wt = fminf(expf(Tg[s]), kLossWeightCap);
+    loss += wt * e * e;
     const float sig = 1.f / (1.f + expf(-z));
-    dz[s] = static_cast<float>(2.0 * inv_batch) * e * sig / sp;
+    dz[s] = static_cast<float>(2.0 * inv_batch) * wt * e * sig / sp;
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);

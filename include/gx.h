@@ -231,7 +231,8 @@ gx_status gx_mlp_set_params(gx_mlp* m, const float* params, const float* norm);
  * set, with targets log(N * r_v) of standard PageRank run to `tolerance`. */
 gx_status gx_mlp_add_graph(gx_mlp* m, gx_engine* e, int32_t max_samples, int32_t max_iter,
                            double tolerance);
-/* Adam on the squared error of log softplus(z) against the targets. */
+/* Adam on the squared error of log softplus(z) against the targets,
+ * weighted by min(N * r_v, 100). */
 gx_status gx_mlp_train(gx_mlp* m, int32_t epochs, int32_t batch, double lr, double* final_loss);
 /* Gradient of the mean loss over n samples (raw features x[n][6], targets
  * t[n]) at the current weights, float[gx_mlp_num_params()]. */

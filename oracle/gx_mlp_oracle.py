@@ -47,7 +47,7 @@ def softplus(z):
 
 
 def loss_and_grad(params, norm, x_raw, t):
-    """Mean over samples of (log softplus(z) - t)^2 and its gradient."""
+    """Mean over samples of min(exp(t), 100) * (log softplus(z) - t)^2 and its gradient."""
     W1, b1, W2, b2, w3, b3 = unpack(params)
     p32 = np.asarray(params, np.float32)
     W1r = bf16_round(p32[:H * F]).reshape(H, F)
@@ -65,8 +65,9 @@ def loss_and_grad(params, norm, x_raw, t):
     sp = softplus(z)
     y = np.log(sp)
     e = y - t
-    loss = np.mean(e * e)
-    dz = 2 * e / n * (1 / (1 + np.exp(-z))) / sp
+    wt = np.minimum(np.exp(t), 100.0)
+    loss = np.mean(wt * e * e)
+    dz = 2 * wt * e / n * (1 / (1 + np.exp(-z))) / sp
     g_w3 = H2.T @ dz
     g_b3 = dz.sum()
     D2 = dz[:, None] * w3r[None, :] * gelu_grad(A2)
