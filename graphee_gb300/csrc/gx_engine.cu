@@ -257,7 +257,7 @@ gx_status alloc_ctl(gx_engine* e) {
 // Decides which shards stay in HBM under the budget (in shard order, like the
 // reference's insert-until-full edge cache, Global.h:170-244), uploads them,
 // and sets up the streaming ring for the rest.
-gx_status plan_shards(gx_engine* e) {
+gx_status plan_shards(gx_engine* e, const int32_t* src_col) {
   const int32_t P = e->P;
   const int64_t per_edge = e->has_weights ? 8 : 4;
   const int64_t budget = e->cfg.cache_budget_bytes;
@@ -284,8 +284,7 @@ gx_status plan_shards(gx_engine* e) {
   if (e->all_resident) {
     GX_TRY(dev_alloc(&e->d_col, static_cast<size_t>(e->E) + 8));
     GX_CUDA(cudaMemset(e->d_col, 0, (e->E + 8) * sizeof(int32_t)));
-    const int32_t* src = e->h_col;
-    GX_CUDA(cudaMemcpy(e->d_col, src, e->E * sizeof(int32_t), cudaMemcpyHostToDevice));
+    GX_CUDA(cudaMemcpy(e->d_col, src_col, e->E * sizeof(int32_t), cudaMemcpyHostToDevice));
     if (e->has_weights) {
       GX_TRY(dev_alloc(&e->d_w, static_cast<size_t>(e->E) + 8));
       GX_CUDA(cudaMemset(e->d_w, 0, (e->E + 8) * sizeof(uint32_t)));
@@ -299,7 +298,7 @@ gx_status plan_shards(gx_engine* e) {
     for (int32_t p = 0; p < P; ++p) {
       if (!e->resident[p]) continue;
       const int64_t n = std::min(hi[p], e->E + 4) - lo[p];
-      GX_CUDA(cudaMemcpy(e->d_col + pos, e->h_col + lo[p], n * sizeof(int32_t), cudaMemcpyHostToDevice));
+      GX_CUDA(cudaMemcpy(e->d_col + pos, src_col + lo[p], n * sizeof(int32_t), cudaMemcpyHostToDevice));
       if (e->has_weights)
         GX_CUDA(cudaMemcpy(e->d_w + pos, e->h_w + lo[p], n * sizeof(uint32_t), cudaMemcpyHostToDevice));
       e->dev_base[p] = pos - lo[p];  // d_col + dev_base[p] is indexed by global edge id
@@ -335,6 +334,20 @@ gx_status build_signatures(gx_engine* e) {
   e->shard_group = (P + 63) / 64;
   GX_TRY(dev_alloc(&e->d_sig, static_cast<size_t>(e->V)));
   GX_CUDA(cudaMemsetAsync(e->d_sig, 0, sizeof(unsigned long long) * e->V, e->s_comp));
+  if (e->all_resident) {
+    // One launch over every edge; each finds its shard from the shards' edge ranges.
+    std::vector<int64_t> ebound(static_cast<size_t>(P) + 1);
+    for (int32_t p = 0; p <= P; ++p) ebound[p] = e->off[e->bounds[p]];
+    int64_t* d_eb = nullptr;
+    GX_TRY(dev_alloc(&d_eb, ebound.size()));
+    GX_CUDA(cudaMemcpy(d_eb, ebound.data(), sizeof(int64_t) * ebound.size(), cudaMemcpyHostToDevice));
+    signature_all_kernel<<<e->n_sm * 8, 256, 0, e->s_comp>>>(e->d_sig, e->d_col, d_eb, P, e->shard_group);
+    cudaError_t err = cudaGetLastError();
+    if (err == cudaSuccess) err = cudaStreamSynchronize(e->s_comp);
+    cudaFree(d_eb);
+    if (err != cudaSuccess) return fail(GX_ERR_CUDA, "signatures: %s", cudaGetErrorString(err));
+    return GX_OK;
+  }
   for (int32_t p = 0; p < P; ++p) {
     const int64_t e0 = e->off[e->bounds[p]], e1 = e->off[e->bounds[p + 1]];
     if (e1 == e0) continue;
@@ -840,12 +853,17 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
 #pragma omp parallel for reduction(| : bad)
   for (int64_t k = 0; k < E; ++k) bad |= (col[k] < 0 || col[k] >= V);
   if (bad) return fail(GX_ERR_INVALID, "gx_load_csc: source id outside [0, %d)", V);
-  // Host copy of the edge data (pinned: it is the streaming source when the
-  // budget does not hold every shard).
-  GX_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->h_col), (E + 8) * sizeof(int32_t), cudaHostAllocDefault));
-  memset(e->h_col + E, 0, 8 * sizeof(int32_t));
+  // Without a shard-cache budget every shard is resident: upload straight
+  // from the caller's array.  With a budget, keep a pinned host copy, the
+  // streaming source of the shards that do not fit.
+  const int32_t* src_col = col;
+  if (e->cfg.cache_budget_bytes >= 0) {
+    GX_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->h_col), (E + 8) * sizeof(int32_t), cudaHostAllocDefault));
+    memset(e->h_col + E, 0, 8 * sizeof(int32_t));
 #pragma omp parallel for schedule(static)
-  for (int64_t k = 0; k < E; ++k) e->h_col[k] = col[k];
+    for (int64_t k = 0; k < E; ++k) e->h_col[k] = col[k];
+    src_col = e->h_col;
+  }
 
   build_units(e);
   GX_TRY(dev_alloc(&e->d_off, static_cast<size_t>(V) + 1));
@@ -879,11 +897,11 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   GX_TRY(dev_alloc(&e->d_frontier, static_cast<size_t>(V)));
   e->n_work = kQueues * (P + 2);
   GX_TRY(dev_alloc(&e->d_work, static_cast<size_t>(e->n_work)));
-  GX_TRY(plan_shards(e));
+  GX_TRY(plan_shards(e, src_col));
   GX_TRY(build_signatures(e));
   if (e->all_resident) {
-    if (e->cfg.layout == 1) GX_TRY(build_blocks(e, e->h_col));
-    cudaFreeHost(e->h_col);
+    if (e->cfg.layout == 1) GX_TRY(build_blocks(e, src_col));
+    if (e->h_col) cudaFreeHost(e->h_col);
     e->h_col = nullptr;
   }
   e->loaded = true;
@@ -919,7 +937,7 @@ gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
       // Need the column data on the host again to re-plan.
       GX_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->h_col), (e->E + 8) * sizeof(int32_t), cudaHostAllocDefault));
       GX_CUDA(cudaMemcpy(e->h_col, e->d_col, (e->E + 8) * sizeof(int32_t), cudaMemcpyDeviceToHost));
-      GX_TRY(plan_shards(e));
+      GX_TRY(plan_shards(e, e->h_col));
       GX_TRY(build_signatures(e));
       if (e->all_resident) {
         cudaFreeHost(e->h_col);
@@ -931,7 +949,7 @@ gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
       GX_CUDA(cudaMemcpy(e->d_w, w, e->E * sizeof(uint32_t), cudaMemcpyHostToDevice));
     }
   } else {
-    GX_TRY(plan_shards(e));
+    GX_TRY(plan_shards(e, e->h_col));
   }
   if (e->all_resident && e->blocks_ready) {
     std::vector<uint32_t> wp(static_cast<size_t>(e->b_edges) + 4, 0u);

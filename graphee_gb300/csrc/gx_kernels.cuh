@@ -753,6 +753,25 @@ static __global__ void signature_kernel(unsigned long long* sig, const int32_t* 
   }
 }
 
+// The same masks for a fully resident graph in one launch: edge k belongs
+// to the shard whose edge range [ebound[p], ebound[p+1]) holds it.
+static __global__ void signature_all_kernel(unsigned long long* sig, const int32_t* col, const int64_t* ebound,
+                                            int32_t P, int32_t group) {
+  const int64_t E = ebound[P];
+  for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < E;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    int lo = 0, hi = P;  // ebound[lo] <= k < ebound[lo + 1]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (ebound[mid] <= k) lo = mid;
+      else hi = mid;
+    }
+    const unsigned long long bit = 1ull << (lo / group);
+    const int u = col[k];
+    if ((sig[u] & bit) == 0) atomicOr(sig + u, bit);
+  }
+}
+
 // Out-edge CSR from the CSC (counting sort by source; order within a source
 // is unspecified, which min-plus / min-label do not observe).
 static __global__ void transpose_kernel(const int64_t* off, const int32_t* col, const uint32_t* w, int n,
