@@ -19,6 +19,7 @@
 #include <omp.h>
 
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -821,6 +822,12 @@ gx_status gx_destroy(gx_engine* e) {
 
 gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds, const int64_t* off,
                       const int32_t* col, const int32_t* outdeg) {
+  const auto t_start = std::chrono::steady_clock::now();
+  auto phase = [&](const char* what) {
+    if (e && e->cfg.verbose)
+      fprintf(stderr, "gx_load_csc %-12s %8.2f ms\n", what,
+              std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_start).count());
+  };
   if (!e) return fail(GX_ERR_INVALID, "gx_load_csc: engine is NULL");
   if (V <= 0 || P <= 0 || !bounds || !off || (off[V] > 0 && !col))
     return fail(GX_ERR_INVALID, "gx_load_csc: bad arguments (V=%d, P=%d)", V, P);
@@ -830,29 +837,42 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   if (off[0] != 0) return fail(GX_ERR_INVALID, "gx_load_csc: off[0] must be 0");
   const int64_t E = off[V];
   if (E > (int64_t(1) << 40)) return fail(GX_ERR_INVALID, "gx_load_csc: too many edges");
-  for (int32_t v = 0; v < V; ++v)
-    if (off[v] > off[v + 1]) return fail(GX_ERR_INVALID, "gx_load_csc: off not monotone at %d", v);
   GX_CUDA(cudaSetDevice(e->dev));
   e->release_graph();
   e->V = V;
   e->P = P;
   e->E = E;
   e->bounds.assign(bounds, bounds + P + 1);
-  e->off.assign(off, off + V + 1);
-  e->outdeg.assign(V, 0);
+  e->off.resize(static_cast<size_t>(V) + 1);
+  e->outdeg.resize(static_cast<size_t>(V));
+  int64_t* hoff = e->off.data();
+#pragma omp parallel for schedule(static)
+  for (int64_t v = 0; v <= V; ++v) hoff[v] = off[v];
   if (outdeg) {
-    memcpy(e->outdeg.data(), outdeg, sizeof(int32_t) * V);
+    int32_t* hod = e->outdeg.data();
+#pragma omp parallel for schedule(static)
+    for (int64_t v = 0; v < V; ++v) hod[v] = outdeg[v];
   } else {
     gx_status st = gx_out_degree(V, off, col, e->outdeg.data());
     if (st != GX_OK) return st;
   }
-  e->n_dangling = 0;
-  for (int32_t v = 0; v < V; ++v) e->n_dangling += e->outdeg[v] == 0;
-  // Validate source ids once on the host (the kernels index vertex arrays with them).
-  int bad = 0;
+  int64_t n_dang = 0;
+#pragma omp parallel for reduction(+ : n_dang)
+  for (int32_t v = 0; v < V; ++v) n_dang += e->outdeg[v] == 0;
+  e->n_dangling = n_dang;
+  // With a shard-cache budget not every shard reaches the device: check the
+  // source ids on the host.  Otherwise the device checks them after the
+  // upload, before any kernel indexes with them.
+  if (e->cfg.cache_budget_bytes >= 0) {
+    int bad = 0;
 #pragma omp parallel for reduction(| : bad)
-  for (int64_t k = 0; k < E; ++k) bad |= (col[k] < 0 || col[k] >= V);
-  if (bad) return fail(GX_ERR_INVALID, "gx_load_csc: source id outside [0, %d)", V);
+    for (int32_t v = 0; v < V; ++v) bad |= off[v] > off[v + 1];
+    if (bad) return fail(GX_ERR_INVALID, "gx_load_csc: off is not non-decreasing");
+#pragma omp parallel for reduction(| : bad)
+    for (int64_t k = 0; k < E; ++k) bad |= (col[k] < 0 || col[k] >= V);
+    if (bad) return fail(GX_ERR_INVALID, "gx_load_csc: source id outside [0, %d)", V);
+  }
+  phase("validated");
   // Without a shard-cache budget every shard is resident: upload straight
   // from the caller's array.  With a budget, keep a pinned host copy, the
   // streaming source of the shards that do not fit.
@@ -866,6 +886,7 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   }
 
   build_units(e);
+  phase("units");
   GX_TRY(dev_alloc(&e->d_off, static_cast<size_t>(V) + 1));
   GX_CUDA(cudaMemcpy(e->d_off, off, sizeof(int64_t) * (V + 1), cudaMemcpyHostToDevice));
   GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
@@ -897,8 +918,32 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   GX_TRY(dev_alloc(&e->d_frontier, static_cast<size_t>(V)));
   e->n_work = kQueues * (P + 2);
   GX_TRY(dev_alloc(&e->d_work, static_cast<size_t>(e->n_work)));
+  phase("vertex arrays");
   GX_TRY(plan_shards(e, src_col));
+  {
+    // Offsets non-decreasing, and (fully resident) every source id in range.
+    unsigned int* flag = nullptr;
+    GX_TRY(dev_alloc(&flag, 1));
+    GX_CUDA(cudaMemsetAsync(flag, 0, sizeof(unsigned int), e->s_comp));
+    validate_csc_kernel<<<e->n_sm * 8, 256, 0, e->s_comp>>>(e->d_off, V, e->all_resident ? e->d_col : nullptr, E,
+                                                             flag);
+    unsigned int h = 0;
+    cudaError_t err = cudaMemcpyAsync(&h, flag, sizeof(h), cudaMemcpyDeviceToHost, e->s_comp);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(e->s_comp);
+    cudaFree(flag);
+    if (err != cudaSuccess) return fail(GX_ERR_CUDA, "gx_load_csc validation: %s", cudaGetErrorString(err));
+    if (h & 1u) {
+      e->release_graph();
+      return fail(GX_ERR_INVALID, "gx_load_csc: off is not non-decreasing");
+    }
+    if (h & 2u) {
+      e->release_graph();
+      return fail(GX_ERR_INVALID, "gx_load_csc: source id outside [0, %d)", V);
+    }
+  }
+  phase("edges");
   GX_TRY(build_signatures(e));
+  phase("signatures");
   if (e->all_resident) {
     if (e->cfg.layout == 1) GX_TRY(build_blocks(e, src_col));
     if (e->h_col) cudaFreeHost(e->h_col);

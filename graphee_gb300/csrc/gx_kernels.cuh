@@ -122,10 +122,15 @@ __device__ __forceinline__ uint32_t sat_add(uint32_t a, uint32_t b) {
 
 // Candidate an in-edge (u -> v) offers v: PageRank contribution, or the
 // min-plus / min-label candidate.
+#ifndef GX_GATHER_CG
+#define GX_GATHER_CG 0
+#endif
+
 template <int APP>
 __device__ __forceinline__ typename AppTraits<APP>::T edge_value(const PullArgs& a, const void* src_val,
                                                                  const float* src_con, int32_t u, uint32_t wt) {
   if constexpr (is_pr<APP>()) {
+    if (GX_GATHER_CG) return __ldcg(src_con + u);
     return __ldg(src_con + u);
   } else if constexpr (APP == K_SSSP_UNIT) {
     return __ldg(static_cast<const int32_t*>(src_val) + u) + 1;  // sssp.cpp:43
@@ -770,6 +775,19 @@ static __global__ void signature_all_kernel(unsigned long long* sig, const int32
     const int u = col[k];
     if ((sig[u] & bit) == 0) atomicOr(sig + u, bit);
   }
+}
+
+// Load-time checks before any kernel indexes with the data: bit 0 set when
+// off decreases somewhere, bit 1 when a source id lies outside [0, V).
+static __global__ void validate_csc_kernel(const int64_t* off, int32_t V, const int32_t* col, int64_t E,
+                                           unsigned int* flag) {
+  const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  const int64_t nt = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  unsigned int f = 0;
+  for (int64_t v = tid; v < V; v += nt) f |= off[v] > off[v + 1] ? 1u : 0u;
+  if (col)
+    for (int64_t k = tid; k < E; k += nt) f |= (col[k] < 0 || col[k] >= V) ? 2u : 0u;
+  if (f) atomicOr(flag, f);
 }
 
 // Out-edge CSR from the CSC (counting sort by source; order within a source

@@ -337,3 +337,22 @@ def test_cpp_app_drivers_vs_oracle(tmp_path):
     d2 = gx.write_shards(s, tmp_path / "t")
     r = subprocess.run([app, "tc", d2, str(s.V), str(s.P), "0"], check=True, capture_output=True, text=True)
     assert int(r.stdout.strip()) == O.triangles(s.V, s.off, s.col)
+
+
+@pytest.mark.parametrize("budget", [-1, 1 << 20])
+def test_load_rejects_bad_csc(budget):
+    g = gx.rmat_graph(10, 8, seed=3, P=4)
+    col = g.col.copy()
+    col[17] = g.V + 5
+    bad = gx.Graph(g.V, g.off, col, g.outdeg, g.P, g.bounds)
+    with gx.Engine(cache_budget_bytes=budget) as e:
+        with pytest.raises(gx.GxError) as ei:
+            e.load(bad)
+        assert ei.value.status == gx.GX_ERR_INVALID and "source id" in str(ei.value)
+        off = g.off.copy()
+        off[100], off[101] = off[101], off[100] - 1
+        with pytest.raises(gx.GxError) as ei:
+            e.load(gx.Graph(g.V, off, g.col, g.outdeg, g.P, g.bounds))
+        assert ei.value.status == gx.GX_ERR_INVALID
+        e.load(g)                      # the engine is still usable
+        assert e.run(gx.APP_CC, 100)["iterations"] > 0
