@@ -166,6 +166,7 @@ __global__ void __launch_bounds__(kBlockThreads, GX_BLOCK_MIN_BLOCKS) pull_block
   c.inv_n = ctl->inv_n;
   c.fx_scale = ctl->fx_scale;
   c.base = ctl->base;
+  c.outdeg = ctl->push_ok ? a.outdeg : nullptr;
   const int cur = ctl->cur;
   const int group = ctl->shard_group;
   const unsigned long long smask = ctl->shard_mask;

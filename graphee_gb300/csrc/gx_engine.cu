@@ -9,7 +9,7 @@
 //   val     T[2][V]      Msg / MsgNew as a double buffer (swap instead of copy)
 //   con     f32[2][V]    PageRank contributions Msg[u]/outdeg[u]
 //   units   int2[U]      warp work units, unit_shard int32[U]
-//   bm      u32[V/32+2]  next-frontier bitmap; frontier int2[V]
+//   bm      u32[V/32+2]  next-frontier bitmap; frontier int4[V+E/256+1] (push only)
 //   sig     u64[V]       per-vertex shard-group mask (selective scheduling)
 //   ooff/ocol/ow         out-edge CSR for sparse push steps (SSSP/CC)
 // With a shard-cache budget, only the shards that fit stay in HBM; the others
@@ -382,6 +382,10 @@ gx_status build_out_edges(gx_engine* e, bool weighted) {
   if (ooff[V] != e->E)
     return fail(GX_ERR_FORMAT, "vertexout.npy sums to %lld out-edges but the shards hold %lld edges",
                 static_cast<long long>(ooff[V]), static_cast<long long>(e->E));
+  // Push frontier: one entry per kPushChunk out-edges of each vertex, so
+  // V + E / kPushChunk + 1 entries hold any frontier.
+  e->frontier_cap = static_cast<unsigned long long>(V) + static_cast<unsigned long long>(e->E) / kPushChunk + 1;
+  if (!e->d_frontier) GX_TRY(dev_alloc(&e->d_frontier, static_cast<size_t>(e->frontier_cap)));
   GX_TRY(dev_alloc(&e->d_ooff, static_cast<size_t>(V) + 1));
   GX_TRY(dev_alloc(&e->d_ocol, static_cast<size_t>(e->E) + 8));
   if (weighted) GX_TRY(dev_alloc(&e->d_ow, static_cast<size_t>(e->E) + 8));
@@ -413,7 +417,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   const int32_t V = e->V;
   const bool weighted = APP == K_SSSP_W;
   const bool min_app = APP == K_SSSP_UNIT || APP == K_SSSP_W || APP == K_CC;
-  const bool push_ok = min_app && e->cfg.push_sparse && e->all_resident;
+  const bool push_ok = min_app && e->cfg.push_sparse && e->all_resident &&
+                       static_cast<int64_t>(V) + e->E / kPushChunk + 1 < INT32_MAX;
   if (push_ok) GX_TRY(build_out_edges(e, weighted));
   if (e->stats_cap < prm.max_iter) {
     GX_TRY(dev_alloc(&e->d_stats, static_cast<size_t>(std::max(prm.max_iter, 1))));
@@ -427,6 +432,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   c.n_shards = e->P;
   c.shard_group = e->shard_group;
   c.push_ok = push_ok;
+  c.push_edge_limit =
+      push_ok ? static_cast<unsigned long long>(e->cfg.push_edge_fraction * static_cast<double>(e->E)) : 0ull;
   c.damping = prm.damping;
   c.inv_n = 1.0 / V;
   c.fx_scale = static_cast<double>(V) * 1073741824.0;  // 2^30 per 1/N of rank
@@ -463,6 +470,20 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
     if (e->device_init) D = e->device_init_dangling;
     c.base = (1.0 - prm.damping) * c.inv_n + prm.damping * D * c.inv_n;
   }
+  // SSSP from init_vertex: only the source holds a finite distance, so step 0
+  // is a push from it (the same values as the reference's full first pull).
+  std::vector<int4> src_entries;
+  if (push_ok && (APP == K_SSSP_UNIT || APP == K_SSSP_W) && !use_init && c.push_edge_limit > 0 &&
+      prm.max_iter > 0) {
+    const int32_t od = e->outdeg[prm.source];
+    for (int32_t k = 0; k < od; k += kPushChunk) src_entries.push_back(make_int4(prm.source, 0, k, 0));
+    c.step0_push = 1;
+    c.mode = MODE_PUSH;
+    c.n_frontier = static_cast<int>(src_entries.size());
+    if (!src_entries.empty())
+      GX_CUDA(cudaMemcpyAsync(e->d_frontier, src_entries.data(), sizeof(int4) * src_entries.size(),
+                              cudaMemcpyHostToDevice, e->s_comp));
+  }
   GX_CUDA(cudaMemcpyAsync(e->d_ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, e->s_comp));
   init_kernel<APP><<<e->n_sm * 4, 256, 0, e->s_comp>>>(e->d_ctl, e->d_val[0], e->d_con[0], e->d_outdeg, V,
                                                        prm.source, use_init);
@@ -498,6 +519,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   qa.ow = e->d_ow;
   qa.val[0] = e->d_val[0];
   qa.val[1] = e->d_val[1];
+  qa.outdeg = e->d_outdeg;
   qa.frontier = e->d_frontier;
   qa.ctr = e->d_work + kQueues;
   qa.bm = e->d_bm;
@@ -509,7 +531,9 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   fa.sig = e->d_sig;
   fa.val[0] = e->d_val[0];
   fa.val[1] = e->d_val[1];
+  fa.outdeg = e->d_outdeg;
   fa.frontier = e->d_frontier;
+  fa.frontier_cap = e->frontier_cap;
   fa.work_ctr = e->d_work;
   fa.n_work_ctr = e->n_work;
 
@@ -716,6 +740,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   float ms = 0;
   GX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
 
+  if (e->h_ctl->error == 2) return fail(GX_ERR_CUDA, "gx_run: push frontier overflow");
   const int32_t steps = e->h_ctl->step;
   e->last_steps = steps;
   e->last_stats.assign(std::max(steps, 0), StepStats{});
@@ -770,6 +795,7 @@ void gx_config_default(gx_config* cfg) {
   cfg->verbose = 0;
   cfg->profile = 0;
   cfg->layout = 0;
+  cfg->push_edge_fraction = 0.5;
 }
 
 void gx_run_params_default(gx_run_params* p, gx_app app) {
@@ -796,6 +822,8 @@ gx_status gx_create(const gx_config* cfg, gx_engine** out) {
     return fail(GX_ERR_NODEVICE, "no CUDA device visible (%s)", cudaGetErrorString(err));
   }
   if (c.device < 0 || c.device >= n) return fail(GX_ERR_INVALID, "device %d out of range [0,%d)", c.device, n);
+  if (!(c.push_edge_fraction >= 0.0 && c.push_edge_fraction <= 1.0))
+    return fail(GX_ERR_INVALID, "push_edge_fraction %g outside [0,1]", c.push_edge_fraction);
   std::unique_ptr<gx_engine> e(new gx_engine());
   e->cfg = c;
   e->dev = c.device;
@@ -915,7 +943,6 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   GX_TRY(dev_alloc(&e->d_hticket, e->heavy.size()));
   e->n_words = (V + 31) / 32 + 2;
   GX_TRY(dev_alloc(&e->d_bm, static_cast<size_t>(e->n_words)));
-  GX_TRY(dev_alloc(&e->d_frontier, static_cast<size_t>(V)));
   e->n_work = kQueues * (P + 2);
   GX_TRY(dev_alloc(&e->d_work, static_cast<size_t>(e->n_work)));
   phase("vertex arrays");

@@ -111,7 +111,8 @@ struct gx_engine {
   uint32_t* d_bm = nullptr;
   int32_t n_words = 0;
   unsigned long long* d_sig = nullptr;
-  int2* d_frontier = nullptr;
+  int4* d_frontier = nullptr;
+  unsigned long long frontier_cap = 0;
   int64_t* d_ooff = nullptr;
   int32_t* d_ocol = nullptr;
   uint32_t* d_ow = nullptr;

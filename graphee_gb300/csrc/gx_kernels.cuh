@@ -23,6 +23,7 @@ constexpr int kWarps = kThreads / 32;
 constexpr int kChunk = 256;             // edges staged per warp per round
 constexpr int kGpsInf = 10000;          // GPS_INF, GraphMP/system/Global.h:50
 constexpr uint32_t kInfW = 0xFFFFFFFFu; // INF of weighted SSSP
+constexpr int kPushChunk = 256;         // out-edges per push frontier entry (longer lists get several)
 
 struct StepStats {
   unsigned long long changed;  // reference _Changed_Vertex
@@ -42,7 +43,8 @@ struct Ctl {
   int n_shards;
   int shard_group;          // shards per bit of the 64-bit shard mask
   int push_ok;              // out-edges resident: sparse steps may push
-  int pad0;
+  int step0_push;           // SSSP from init_vertex: step 0 pushes from the source alone
+  unsigned long long push_edge_limit;  // push when the frontier has at most this many out-edges
   double damping;
   double inv_n;             // 1.0 / N, as the reference computes it
   double fx_scale;          // fixed-point scale of resid_fx / dangl_fx
@@ -59,6 +61,7 @@ struct Ctl {
   unsigned long long shard_mask;       // active shard groups, current step
   unsigned long long shard_mask_next;  // being built by finalize
   unsigned long long changed, active, edges, resid_fx, dangl_fx;  // current-step accumulators
+  unsigned long long front_edges;      // out-edges of the vertices that changed this step
   unsigned int next_frontier;
   unsigned int fin_ticket;
 };
@@ -88,7 +91,8 @@ struct PushArgs {
   const int32_t* ocol;      // destinations
   const uint32_t* ow;       // weights aligned with ocol
   void* val[2];
-  const int2* frontier;     // (vertex, value bits) snapshot from the previous step
+  const int32_t* outdeg;
+  const int4* frontier;     // (vertex, value bits, first out-edge of the entry, 0) from the previous step
   unsigned int* ctr;
   uint32_t* bm;
 };
@@ -100,7 +104,9 @@ struct FinArgs {
   int32_t n_words;
   const unsigned long long* sig;  // per-vertex 64-bit mask of shard groups it feeds
   void* val[2];
-  int2* frontier;
+  const int32_t* outdeg;
+  int4* frontier;
+  unsigned long long frontier_cap;  // entries; |frontier| + E / kPushChunk + 1 fit by construction
   unsigned int* work_ctr;
   int32_t n_work_ctr;
 };
@@ -152,10 +158,11 @@ __device__ __forceinline__ typename AppTraits<APP>::T combine(typename AppTraits
 struct ApplyCtx {
   int step;
   double damping, inv_n, fx_scale, base;
+  const int32_t* outdeg;  // min apps that may push: sum the out-degree of changed vertices
 };
 
 struct LocalAcc {
-  unsigned long long changed = 0, active = 0, edges = 0, resid = 0, dangl = 0;
+  unsigned long long changed = 0, active = 0, edges = 0, resid = 0, dangl = 0, fedges = 0;
 };
 
 // Apply step for vertex v given its gathered value (end of comp_* + end_comp):
@@ -188,6 +195,9 @@ __device__ __forceinline__ bool apply_vertex(const ApplyCtx c, int v, typename A
   la.changed += (nv != prev);
   const bool act = nv != old;
   la.active += act;  // not reported from here; finalize recounts from the bitmap
+  if constexpr (!is_pr<APP>()) {
+    if (act && c.outdeg) la.fedges += static_cast<unsigned long long>(__ldg(c.outdeg + v));
+  }
   return act;
 }
 
@@ -258,24 +268,26 @@ __device__ __forceinline__ typename AppTraits<APP>::T identity() {
 }
 
 __device__ __forceinline__ void flush_block(Ctl* ctl, const LocalAcc& la) {
-  __shared__ unsigned long long s_red[4][kWarps];
+  __shared__ unsigned long long s_red[5][kWarps];
   unsigned long long ch = warp_sum(la.changed), ed = warp_sum(la.edges), rs = warp_sum(la.resid),
-                     dg = warp_sum(la.dangl);
+                     dg = warp_sum(la.dangl), fe = warp_sum(la.fedges);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (lane == 0) {
     s_red[0][wid] = ch;
     s_red[1][wid] = ed;
     s_red[2][wid] = rs;
     s_red[3][wid] = dg;
+    s_red[4][wid] = fe;
   }
   __syncthreads();
-  if (threadIdx.x < 4) {
+  if (threadIdx.x < 5) {
     unsigned long long t = 0;
     for (int i = 0; i < kWarps; ++i) t += s_red[threadIdx.x][i];
     unsigned long long* dst = threadIdx.x == 0 ? &ctl->changed
                             : threadIdx.x == 1 ? &ctl->edges
                             : threadIdx.x == 2 ? &ctl->resid_fx
-                                               : &ctl->dangl_fx;
+                            : threadIdx.x == 3 ? &ctl->dangl_fx
+                                               : &ctl->front_edges;
     if (t) atomicAdd(dst, t);
   }
 }
@@ -332,6 +344,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
   c.inv_n = ctl->inv_n;
   c.fx_scale = ctl->fx_scale;
   c.base = ctl->base;
+  c.outdeg = ctl->push_ok ? a.outdeg : nullptr;
   const int cur = ctl->cur;
   const int group = ctl->shard_group;
   const unsigned long long smask = ctl->shard_mask;
@@ -577,7 +590,12 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
 // Push (sparse steps of SSSP/CC): each frontier vertex u, with the value it
 // held at the end of the previous step, relaxes its out-edges with atomicMin.
 // For min-plus / min-label this equals the Jacobi pull of the reference:
-// a vertex whose in-neighbours did not change cannot improve.
+// a vertex whose in-neighbours did not change cannot improve, so the values
+// and the per-step change counts are those of a full pull.
+// Frontier entries cover at most kPushChunk out-edges each (a hub is several
+// entries).  A warp claims 32 entries and sweeps their concatenated edge
+// ranges 32 edges at a time; each lane finds the entry that owns its edge by
+// a binary search over the warp's exclusive prefix sums.
 // ---------------------------------------------------------------------------
 template <int APP>
 __global__ void __launch_bounds__(kThreads) push_kernel(PushArgs a) {
@@ -595,25 +613,53 @@ __global__ void __launch_bounds__(kThreads) push_kernel(PushArgs a) {
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= nf) break;
     const int cnt = nf - base < 32 ? nf - base : 32;
-    int2 my = make_int2(0, 0);
-    if (lane < cnt) my = a.frontier[base + lane];
-    for (int j = 0; j < cnt; ++j) {
-      const int u = __shfl_sync(0xffffffffu, my.x, j);
-      const T su = static_cast<T>(__shfl_sync(0xffffffffu, my.y, j));
-      const int64_t b = a.ooff[u], e = a.ooff[u + 1];
-      if (lane == 0) la.edges += e - b;
-      for (int64_t k = b + lane; k < e; k += 32) {
-        const int vtx = __ldcs(a.ocol + k);
+    int d = 0;
+    uint32_t su = 0;
+    long long b = 0;
+    if (lane < cnt) {
+      const int4 f = a.frontier[base + lane];
+      su = static_cast<uint32_t>(f.y);
+      b = a.ooff[f.x] + f.z;
+      const long long left = a.ooff[f.x + 1] - b;
+      d = static_cast<int>(left < kPushChunk ? left : kPushChunk);
+    }
+    int incl = d;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    const int total = __shfl_sync(0xffffffffu, incl, 31);
+    const int excl = incl - d;
+    la.edges += static_cast<unsigned long long>(d);
+    for (int k0 = 0; k0 < total; k0 += 32) {
+      const int k = k0 + lane;
+      // Largest j with excl[j] <= k; that entry has d[j] > 0 when k < total.
+      int j = 0;
+#pragma unroll
+      for (int sp = 16; sp > 0; sp >>= 1) {
+        const int ex = __shfl_sync(0xffffffffu, excl, j + sp);
+        if (ex <= k) j += sp;
+      }
+      const int exj = __shfl_sync(0xffffffffu, excl, j);
+      const long long bj = __shfl_sync(0xffffffffu, b, j);
+      const uint32_t sj = __shfl_sync(0xffffffffu, su, j);
+      if (k < total) {
+        const long long edge = bj + (k - exj);
+        const int vtx = __ldcs(a.ocol + edge);
         T cand;
-        if constexpr (APP == K_SSSP_UNIT) cand = su + 1;
-        else if constexpr (APP == K_SSSP_W) cand = sat_add(static_cast<uint32_t>(su), __ldcs(a.ow + k));
-        else cand = su;
+        if constexpr (APP == K_SSSP_UNIT) cand = static_cast<T>(sj) + 1;
+        else if constexpr (APP == K_SSSP_W) cand = sat_add(sj, __ldcs(a.ow + edge));
+        else cand = static_cast<T>(sj);
         if (cand < val[vtx]) {
           const T prev = atomicMin(val + vtx, cand);
           if (cand < prev) {
             const uint32_t bit = 1u << (vtx & 31);
             const uint32_t was = atomicOr(a.bm + (vtx >> 5), bit);
-            if (!(was & bit)) la.changed += 1;
+            if (!(was & bit)) {
+              la.changed += 1;
+              la.fedges += static_cast<unsigned long long>(__ldg(a.outdeg + vtx));
+            }
           }
         }
       }
@@ -640,29 +686,63 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
   Ctl* ctl = a.ctl;
   const Ctl c = *ctl;
   if (c.done) return;
+  // A step-0 push from the SSSP source alone stands for the reference's
+  // full first pull, whose _Changed_Vertex compares against VertexValue = 0:
+  // every vertex but the source ends with a non-zero distance.
+  const unsigned long long changed =
+      (c.step == 0 && c.step0_push) ? static_cast<unsigned long long>(c.n_vertices - 1) : c.changed;
   // updated_ratio is a float in the reference (GraphPS.h:203,297).
-  const float ratio = static_cast<float>(static_cast<double>(c.changed) / c.n_vertices);
+  const float ratio = static_cast<float>(static_cast<double>(changed) / c.n_vertices);
   const bool sel_next = static_cast<double>(ratio) < c.sel_threshold;
-  const bool push_next = sel_next && c.push_ok;
+  // Push is exact for min apps whatever the frontier size; beyond the
+  // reference's selective steps it is chosen when the frontier's out-edges
+  // are few enough to beat a full pull.
+  const bool push_next = c.push_ok && (sel_next || c.front_edges <= c.push_edge_limit);
   const bool want_mask = sel_next && !push_next && a.sig != nullptr;
   const int nb = c.mode == MODE_PUSH ? c.cur : (c.cur ^ 1);
   const T* newv = static_cast<const T*>(nb ? a.val[1] : a.val[0]);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   unsigned long long act = 0, mask = 0;
-  for (int w = blockIdx.x * kThreads + threadIdx.x; w < a.n_words; w += gridDim.x * kThreads) {
-    uint32_t word = a.bm[w];
-    if (!word) continue;
-    a.bm[w] = 0;
-    act += __popc(word);
-    if (want_mask) {
-      for (uint32_t x = word; x; x &= x - 1) mask |= a.sig[(w << 5) + __ffs(x) - 1];
+  // Warp-uniform sweep: lane i takes word w0 + i, so the frontier compaction
+  // can reserve its slots with one atomic per warp.
+  for (int w0 = blockIdx.x * kThreads + (wid << 5); w0 < a.n_words; w0 += gridDim.x * kThreads) {
+    const int w = w0 + lane;
+    const uint32_t word = w < a.n_words ? a.bm[w] : 0u;
+    if (word) {
+      a.bm[w] = 0;
+      act += __popc(word);
+      if (want_mask) {
+        for (uint32_t x = word; x; x &= x - 1) mask |= a.sig[(w << 5) + __ffs(x) - 1];
+      }
     }
     if (push_next) {
+      unsigned n_ent = 0;
       for (uint32_t x = word; x; x &= x - 1) {
-        const int u = (w << 5) + __ffs(x) - 1;
-        const unsigned pos = atomicAdd(&ctl->next_frontier, 1u);
-        T vu = newv[u];
-        a.frontier[pos] = make_int2(u, *reinterpret_cast<int*>(&vu));
+        const int od = __ldg(a.outdeg + (w << 5) + __ffs(x) - 1);
+        n_ent += static_cast<unsigned>((od + kPushChunk - 1) / kPushChunk);  // sinks need no entry
+      }
+      unsigned incl = n_ent;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const unsigned tot = __shfl_sync(0xffffffffu, incl, 31);
+      if (tot) {
+        unsigned wbase = 0;
+        if (lane == 31) wbase = atomicAdd(&ctl->next_frontier, tot);
+        wbase = __shfl_sync(0xffffffffu, wbase, 31);
+        unsigned long long pos = static_cast<unsigned long long>(wbase) + (incl - n_ent);
+        for (uint32_t x = word; x; x &= x - 1) {
+          const int u = (w << 5) + __ffs(x) - 1;
+          const int od = __ldg(a.outdeg + u);
+          T vu = newv[u];
+          const int bits = *reinterpret_cast<int*>(&vu);
+          for (int k = 0; k < od; k += kPushChunk, ++pos) {
+            if (pos < a.frontier_cap) a.frontier[pos] = make_int4(u, bits, k, 0);
+            else ctl->error = 2;
+          }
+        }
       }
     }
   }
@@ -692,7 +772,7 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
   if (threadIdx.x == 0) {
     volatile Ctl* vc = ctl;
     StepStats s;
-    s.changed = vc->changed;
+    s.changed = changed;
     s.active = vc->active;
     s.edges = vc->edges;
     s.resid_fx = vc->resid_fx;
@@ -710,6 +790,7 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
     ctl->shard_mask_next = 0;
     ctl->n_frontier = static_cast<int>(vc->next_frontier);
     ctl->next_frontier = 0;
+    ctl->front_edges = 0;
     if (APP == K_PR_STD) {
       const double D = static_cast<double>(s.dangl_fx) / c.fx_scale;
       ctl->base = (1.0 - c.damping) * c.inv_n + c.damping * D * c.inv_n;

@@ -170,7 +170,9 @@ extern "C" gx_status gx_pagerank_noalloc(const int64_t* d_off, const int32_t* d_
   fa.sig = nullptr;
   fa.val[0] = d_rank;
   fa.val[1] = s->val1;
+  fa.outdeg = nullptr;
   fa.frontier = nullptr;  // never written: push steps are off
+  fa.frontier_cap = 0;
   fa.work_ctr = s->work;
   fa.n_work_ctr = kNoAllocWork;
   // Steps after termination return at once; no host round trip per step.

@@ -137,16 +137,39 @@ def test_pagerank_std_vs_fp64():
     assert e.iter_stats(its - 1)["residual_l1"] < 1e-6
 
 
-def test_sssp_weighted_vs_oracle():
+# (push_sparse, push_edge_fraction): reference scheduling only, the default
+# frontier-size rule, and push on every step.
+PUSH_RULES = [(1, 0.5), (1, 0.0), (1, 1.0), (0, 0.5)]
+
+
+@pytest.mark.parametrize("push,frac", PUSH_RULES)
+def test_sssp_weighted_vs_oracle(push, frac):
     g = gx.rmat_graph(15, 16, seed=7, P=8, weight_seed=99)
     ref, ch, _ = O.run(O.SSSP, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 1000, weights=g.weights, source=0)
-    for push in (1, 0):
-        e = engine_for(g, push_sparse=push)
-        st = e.run(gx.APP_SSSP, 1000, source=0, weighted=True)
-        assert np.array_equal(e.values(), ref)
-        assert np.array_equal(run_changed(e, st["iterations"]), ch)
-        if push:
-            assert st["push_iterations"] > 0
+    e = engine_for(g, push_sparse=push, push_edge_fraction=frac)
+    st = e.run(gx.APP_SSSP, 1000, source=0, weighted=True)
+    assert np.array_equal(e.values(), ref)
+    assert np.array_equal(run_changed(e, st["iterations"]), ch)
+    if push:
+        assert st["push_iterations"] > 0
+    if push and frac == 1.0:
+        assert st["push_iterations"] == st["iterations"]
+
+
+@pytest.mark.parametrize("push,frac", PUSH_RULES)
+def test_sssp_unit_and_cc_push_rules_vs_oracle(push, frac):
+    g = gx.rmat_graph(14, 16, seed=21, P=8)
+    ref, ch, _ = O.run(O.SSSP, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 1000, source=3)
+    e = engine_for(g, push_sparse=push, push_edge_fraction=frac)
+    st = e.run(gx.APP_SSSP, 1000, source=3)
+    assert np.array_equal(e.values(), ref)
+    assert np.array_equal(run_changed(e, st["iterations"]), ch)
+    gs = gx.rmat_graph(14, 8, seed=22, P=8, symmetric=True)
+    ref, ch, _ = O.run(O.CC, gs.V, gs.P, gs.bounds, gs.off, gs.col, gs.outdeg, 1000)
+    e = engine_for(gs, push_sparse=push, push_edge_fraction=frac)
+    st = e.run(gx.APP_CC, 1000)
+    assert np.array_equal(e.values(), ref)
+    assert np.array_equal(run_changed(e, st["iterations"]), ch)
 
 
 def test_cc_symmetric_rmat_vs_oracle():
