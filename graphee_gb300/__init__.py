@@ -107,6 +107,7 @@ def lib() -> C.CDLL:
         "gx_last_error": (C.c_char_p, []),
         "gx_create": (C.c_int, [P, P]),
         "gx_destroy": (C.c_int, [P]),
+        "gx_release_cached_memory": (C.c_int, [I32]),
         "gx_load_shards": (C.c_int, [P, C.c_char_p, I32, I32]),
         "gx_load_csc": (C.c_int, [P, I32, I32, P, P, P, P]),
         "gx_set_weights": (C.c_int, [P, P]),
@@ -299,6 +300,11 @@ def batch_graph(n: int, scales=(10, 17), edge_factors=(8, 32), seed: int = 1, a=
 
 # ---------------------------------------------------------------- engine ----
 
+def release_cached_memory(device: int = 0) -> None:
+    """Returns the device memory engines keep cached after close()."""
+    _check(lib().gx_release_cached_memory(device), "gx_release_cached_memory")
+
+
 def default_config(**kw) -> Config:
     cfg = Config()
     lib().gx_config_default(C.byref(cfg))
@@ -377,8 +383,14 @@ class Engine:
         self._weighted = weighted
         return st.as_dict()
 
-    def values(self) -> np.ndarray:
-        out = np.empty(self.V, np.uint32)
+    def values(self, out: np.ndarray | None = None) -> np.ndarray:
+        """The current values; `out` (V 4-byte elements, C-contiguous) is
+        filled and reused instead of a new array."""
+        if out is None:
+            out = np.empty(self.V, np.uint32)
+        elif out.dtype.itemsize != 4 or out.size != self.V or not out.flags.c_contiguous:
+            raise ValueError("values(out=...): need a C-contiguous array of V 4-byte elements")
+        out = out.view(np.uint32)
         _check(lib().gx_get_values(self._h, _ptr(out)), "gx_get_values")
         if self.app in (APP_PAGERANK_REF, APP_PAGERANK_STD):
             return out.view(np.float32)

@@ -28,7 +28,53 @@
 
 #include "gx_engine.h"
 
+#include <mutex>
+
 using namespace gx;
+
+namespace gx {
+
+int current_device() {
+  int d = 0;
+  cudaGetDevice(&d);
+  return d;
+}
+
+static std::mutex g_pool_mu;
+static DevicePool g_pools[64];
+static bool g_pool_tried[64];
+
+DevicePool* device_pool(int dev) {
+  if (dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  if (!g_pool_tried[dev]) {
+    g_pool_tried[dev] = true;
+    int supported = 0;
+    cudaDeviceGetAttribute(&supported, cudaDevAttrMemoryPoolsSupported, dev);
+    if (supported) {
+      cudaMemPoolProps props{};
+      props.allocType = cudaMemAllocationTypePinned;
+      props.handleTypes = cudaMemHandleTypeNone;
+      props.location.type = cudaMemLocationTypeDevice;
+      props.location.id = dev;
+      cudaMemPool_t pool = nullptr;
+      cudaStream_t st = nullptr;
+      if (cudaMemPoolCreate(&pool, &props) == cudaSuccess &&
+          cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) == cudaSuccess) {
+        unsigned long long keep = ~0ull;
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        g_pools[dev].pool = pool;
+        g_pools[dev].stream = st;
+      } else {
+        if (pool) cudaMemPoolDestroy(pool);
+        cudaGetLastError();
+      }
+    }
+  }
+  return g_pools[dev].pool ? &g_pools[dev] : nullptr;
+}
+
+}  // namespace gx
 
 namespace {
 
@@ -70,37 +116,58 @@ void build_units(gx_engine* e) {
     }
     close(t);
   }
-  e->units.clear();
-  e->unit_shard.clear();
-  e->heavy.clear();
-  e->unit_begin.assign(P + 1, 0);
-  int64_t partials = 0;
+  // Per shard: heavy vertices longest first, then counts; the shards' unit
+  // ranges are laid end to end and filled in parallel.
+  std::vector<int64_t> n_units(static_cast<size_t>(P) + 1, 0), n_heavy(static_cast<size_t>(P) + 1, 0),
+      n_part(static_cast<size_t>(P) + 1, 0);
+#pragma omp parallel for schedule(dynamic, 1)
   for (int32_t p = 0; p < P; ++p) {
-    e->unit_begin[p] = static_cast<int32_t>(e->units.size());
-    // Longest heavy vertices first within the shard.
     std::vector<int32_t>& hv = sh[p];
     std::sort(hv.begin(), hv.end(), [&](int32_t a, int32_t b) {
       const int64_t da = off[a + 1] - off[a], db = off[b + 1] - off[b];
       return da > db || (da == db && a < b);
     });
-    for (int32_t v : hv) {
+    int64_t chunks = 0;
+    for (int32_t v : hv) chunks += (off[v + 1] - off[v] + kHeavyChunk - 1) / kHeavyChunk;
+    n_units[p + 1] = chunks + static_cast<int64_t>(su[p].size());
+    n_heavy[p + 1] = static_cast<int64_t>(hv.size());
+    n_part[p + 1] = chunks;
+  }
+  for (int32_t p = 0; p < P; ++p) {
+    n_units[p + 1] += n_units[p];
+    n_heavy[p + 1] += n_heavy[p];
+    n_part[p + 1] += n_part[p];
+  }
+  e->units.resize(static_cast<size_t>(n_units[P]));
+  e->unit_shard.resize(static_cast<size_t>(n_units[P]));
+  e->heavy.resize(static_cast<size_t>(n_heavy[P]));
+  e->unit_begin.assign(P + 1, 0);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int32_t p = 0; p < P; ++p) {
+    int64_t u = n_units[p];
+    int64_t h = n_heavy[p];
+    int64_t part = n_part[p];
+    e->unit_begin[p] = static_cast<int32_t>(u);
+    for (int32_t v : sh[p]) {
       const int64_t d = off[v + 1] - off[v];
       const int32_t nch = static_cast<int32_t>((d + kHeavyChunk - 1) / kHeavyChunk);
-      const int32_t h = static_cast<int32_t>(e->heavy.size());
-      e->heavy.push_back(make_int4(v, nch, static_cast<int32_t>(partials), p));
+      e->heavy[h] = make_int4(v, nch, static_cast<int32_t>(part), p);
       for (int32_t c = 0; c < nch; ++c) {
-        e->units.push_back(make_int2(-(h + 1), c));
-        e->unit_shard.push_back(p);
+        e->units[u] = make_int2(-(static_cast<int32_t>(h) + 1), c);
+        e->unit_shard[u] = p;
+        ++u;
       }
-      partials += nch;
+      part += nch;
+      ++h;
     }
-    for (const int2& u : su[p]) {
-      e->units.push_back(u);
-      e->unit_shard.push_back(p);
+    for (const int2& t : su[p]) {
+      e->units[u] = t;
+      e->unit_shard[u] = p;
+      ++u;
     }
   }
-  e->unit_begin[P] = static_cast<int32_t>(e->units.size());
-  e->n_partials = partials;
+  e->unit_begin[P] = static_cast<int32_t>(n_units[P]);
+  e->n_partials = n_part[P];
 }
 
 // ---- block layout of the default resident pull path (gx_block.cuh) ----
@@ -255,10 +322,44 @@ gx_status alloc_ctl(gx_engine* e) {
   return GX_OK;
 }
 
+// Copies `bytes` (a multiple of 4) from host memory the device reads in place
+// (pageable memory on a system with cudaDevAttrPageableMemoryAccess) to the
+// device, 16 bytes per thread step when both ends are 16-byte aligned.
+__global__ void host_copy_kernel(const void* __restrict__ src, void* __restrict__ dst, size_t bytes) {
+  const size_t stride = static_cast<size_t>(gridDim.x) * blockDim.x;
+  const size_t tid = static_cast<size_t>(blockIdx.x) * blockDim.x + threadIdx.x;
+  size_t done = 0;
+  if (((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15u) == 0) {
+    const size_t n16 = bytes / 16;
+    const int4* s16 = static_cast<const int4*>(src);
+    int4* d16 = static_cast<int4*>(dst);
+    for (size_t i = tid; i < n16; i += stride) d16[i] = s16[i];
+    done = n16 * 16;
+  }
+  const uint32_t* s4 = reinterpret_cast<const uint32_t*>(static_cast<const char*>(src) + done);
+  uint32_t* d4 = reinterpret_cast<uint32_t*>(static_cast<char*>(dst) + done);
+  const size_t n4 = (bytes - done) / 4;
+  for (size_t i = tid; i < n4; i += stride) d4[i] = s4[i];
+}
+
+// Host-to-device copy of a caller's array on `s`: read in place by a kernel
+// when the device can (no staging through pinned buffers, and the host thread
+// is free at once), else cudaMemcpyAsync.
+gx_status upload_async(gx_engine* e, void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return GX_OK;
+  if (e->pageable_access && (reinterpret_cast<uintptr_t>(src) & 3u) == 0 && bytes % 4 == 0) {
+    host_copy_kernel<<<e->n_sm * 8, 256, 0, s>>>(src, dst, bytes);
+    GX_CUDA(cudaGetLastError());
+  } else {
+    GX_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+  }
+  return GX_OK;
+}
+
 // Decides which shards stay in HBM under the budget (in shard order, like the
 // reference's insert-until-full edge cache, Global.h:170-244), uploads them,
 // and sets up the streaming ring for the rest.
-gx_status plan_shards(gx_engine* e, const int32_t* src_col) {
+gx_status plan_shards(gx_engine* e, const int32_t* src_col, bool col_on_device) {
   const int32_t P = e->P;
   const int64_t per_edge = e->has_weights ? 8 : 4;
   const int64_t budget = e->cfg.cache_budget_bytes;
@@ -280,12 +381,14 @@ gx_status plan_shards(gx_engine* e, const int32_t* src_col) {
     }
   }
   e->all_resident = e->n_resident == P;
-  dev_free(&e->d_col);
+  if (!(col_on_device && e->all_resident)) dev_free(&e->d_col);
   dev_free(&e->d_w);
   if (e->all_resident) {
-    GX_TRY(dev_alloc(&e->d_col, static_cast<size_t>(e->E) + 8));
-    GX_CUDA(cudaMemset(e->d_col, 0, (e->E + 8) * sizeof(int32_t)));
-    GX_CUDA(cudaMemcpy(e->d_col, src_col, e->E * sizeof(int32_t), cudaMemcpyHostToDevice));
+    if (!col_on_device) {
+      GX_TRY(dev_alloc(&e->d_col, static_cast<size_t>(e->E) + 8));
+      GX_CUDA(cudaMemset(e->d_col, 0, (e->E + 8) * sizeof(int32_t)));
+      GX_CUDA(cudaMemcpy(e->d_col, src_col, e->E * sizeof(int32_t), cudaMemcpyHostToDevice));
+    }
     if (e->has_weights) {
       GX_TRY(dev_alloc(&e->d_w, static_cast<size_t>(e->E) + 8));
       GX_CUDA(cudaMemset(e->d_w, 0, (e->E + 8) * sizeof(uint32_t)));
@@ -342,7 +445,7 @@ gx_status build_signatures(gx_engine* e) {
     int64_t* d_eb = nullptr;
     GX_TRY(dev_alloc(&d_eb, ebound.size()));
     GX_CUDA(cudaMemcpy(d_eb, ebound.data(), sizeof(int64_t) * ebound.size(), cudaMemcpyHostToDevice));
-    signature_all_kernel<<<e->n_sm * 8, 256, 0, e->s_comp>>>(e->d_sig, e->d_col, d_eb, P, e->shard_group);
+    signature_all_kernel<<<e->n_sm * 8, 256, 0, e->s_comp>>>(e->d_sig, e->d_col, d_eb, P, e->shard_group, e->V);
     cudaError_t err = cudaGetLastError();
     if (err == cudaSuccess) err = cudaStreamSynchronize(e->s_comp);
     cudaFree(d_eb);
@@ -456,17 +559,15 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   if (APP == K_PR_STD) {
     // D of the initial vector, in the same fixed point the device uses.
     double D = 0;
-    int64_t n_dangling = 0;
-    for (int32_t v = 0; v < V; ++v) {
-      if (e->outdeg[v] != 0) continue;
-      ++n_dangling;
-      if (use_init && !e->device_init) {
+    if (use_init && !e->device_init) {
+      for (int32_t v = 0; v < V; ++v) {
+        if (e->outdeg[v] != 0) continue;
         float x;
         memcpy(&x, &e->init_vals[v], sizeof(float));
         D += x;
       }
     }
-    if (!use_init) D = static_cast<double>(n_dangling) * static_cast<double>(static_cast<float>(1.0 / V));
+    if (!use_init) D = static_cast<double>(e->n_dangling) * static_cast<double>(static_cast<float>(1.0 / V));
     if (e->device_init) D = e->device_init_dangling;
     c.base = (1.0 - prm.damping) * c.inv_n + prm.damping * D * c.inv_n;
   }
@@ -829,6 +930,7 @@ gx_status gx_create(const gx_config* cfg, gx_engine** out) {
   e->dev = c.device;
   GX_CUDA(cudaSetDevice(e->dev));
   GX_CUDA(cudaDeviceGetAttribute(&e->n_sm, cudaDevAttrMultiProcessorCount, e->dev));
+  GX_CUDA(cudaDeviceGetAttribute(&e->pageable_access, cudaDevAttrPageableMemoryAccess, e->dev));
   GX_CUDA(cudaStreamCreateWithFlags(&e->s_comp, cudaStreamNonBlocking));
   GX_CUDA(cudaStreamCreateWithFlags(&e->s_copy, cudaStreamNonBlocking));
   e->s_copies.push_back(e->s_copy);
@@ -845,6 +947,23 @@ gx_status gx_create(const gx_config* cfg, gx_engine** out) {
 gx_status gx_destroy(gx_engine* e) {
   if (!e) return GX_OK;
   delete e;
+  return GX_OK;
+}
+
+gx_status gx_release_cached_memory(int32_t device) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n == 0) {
+    cudaGetLastError();
+    return fail(GX_ERR_NODEVICE, "no CUDA device visible");
+  }
+  if (device < 0 || device >= n) return fail(GX_ERR_INVALID, "device %d out of range [0,%d)", device, n);
+  int prev = 0;
+  GX_CUDA(cudaGetDevice(&prev));
+  GX_CUDA(cudaSetDevice(device));
+  DevicePool* dp = device_pool(device);
+  cudaError_t err = dp ? cudaMemPoolTrimTo(dp->pool, 0) : cudaSuccess;
+  cudaSetDevice(prev);
+  if (err != cudaSuccess) return fail(GX_ERR_CUDA, "cudaMemPoolTrimTo: %s", cudaGetErrorString(err));
   return GX_OK;
 }
 
@@ -870,6 +989,49 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   e->V = V;
   e->P = P;
   e->E = E;
+  // Without a shard-cache budget every shard is resident: the offsets, the
+  // out-degrees and the source ids go to the device at once, on the copy
+  // stream, while the host prepares the work units below.
+  const bool direct = e->cfg.cache_budget_bytes < 0;
+  // Small device buffers of the load; freed once the copy stream is idle.
+  struct Scratch {
+    cudaStream_t s;
+    unsigned int* flag = nullptr;
+    int64_t* ebound = nullptr;
+    ~Scratch() {
+      if (flag || ebound) cudaStreamSynchronize(s);
+      dev_free(&flag);
+      dev_free(&ebound);
+    }
+  } scratch{e->s_copy};
+  if (direct) {
+    GX_TRY(dev_alloc(&e->d_off, static_cast<size_t>(V) + 1));
+    GX_TRY(dev_alloc(&e->d_col, static_cast<size_t>(E) + 8));
+    GX_CUDA(cudaMemsetAsync(e->d_col + E, 0, 8 * sizeof(int32_t), e->s_copy));
+    GX_TRY(upload_async(e, e->d_off, off, sizeof(int64_t) * (static_cast<size_t>(V) + 1), e->s_copy));
+    GX_TRY(upload_async(e, e->d_col, col, sizeof(int32_t) * static_cast<size_t>(E), e->s_copy));
+    if (outdeg) {
+      GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
+      GX_TRY(upload_async(e, e->d_outdeg, outdeg, sizeof(int32_t) * static_cast<size_t>(V), e->s_copy));
+    }
+    // Behind the uploads: the load-time checks, then the shard signatures
+    // (whose kernel skips ids the checks will reject).
+    GX_TRY(dev_alloc(&scratch.flag, 1));
+    GX_CUDA(cudaMemsetAsync(scratch.flag, 0, sizeof(unsigned int), e->s_copy));
+    validate_csc_kernel<<<e->n_sm * 8, 256, 0, e->s_copy>>>(e->d_off, V, e->d_col, E, scratch.flag);
+    GX_CUDA(cudaGetLastError());
+    e->shard_group = (P + 63) / 64;
+    GX_TRY(dev_alloc(&e->d_sig, static_cast<size_t>(V)));
+    GX_CUDA(cudaMemsetAsync(e->d_sig, 0, sizeof(unsigned long long) * V, e->s_copy));
+    std::vector<int64_t> ebound(static_cast<size_t>(P) + 1);
+    for (int32_t p = 0; p <= P; ++p) ebound[p] = off[bounds[p]];
+    GX_TRY(dev_alloc(&scratch.ebound, ebound.size()));
+    GX_CUDA(cudaMemcpyAsync(scratch.ebound, ebound.data(), sizeof(int64_t) * ebound.size(), cudaMemcpyHostToDevice,
+                            e->s_copy));
+    signature_all_kernel<<<e->n_sm * 8, 256, 0, e->s_copy>>>(e->d_sig, e->d_col, scratch.ebound, P, e->shard_group,
+                                                              V);
+    GX_CUDA(cudaGetLastError());
+  }
   e->bounds.assign(bounds, bounds + P + 1);
   e->off.resize(static_cast<size_t>(V) + 1);
   e->outdeg.resize(static_cast<size_t>(V));
@@ -915,10 +1077,14 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
 
   build_units(e);
   phase("units");
-  GX_TRY(dev_alloc(&e->d_off, static_cast<size_t>(V) + 1));
-  GX_CUDA(cudaMemcpy(e->d_off, off, sizeof(int64_t) * (V + 1), cudaMemcpyHostToDevice));
-  GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
-  GX_CUDA(cudaMemcpy(e->d_outdeg, e->outdeg.data(), sizeof(int32_t) * V, cudaMemcpyHostToDevice));
+  if (!direct) {
+    GX_TRY(dev_alloc(&e->d_off, static_cast<size_t>(V) + 1));
+    GX_CUDA(cudaMemcpy(e->d_off, off, sizeof(int64_t) * (V + 1), cudaMemcpyHostToDevice));
+  }
+  if (!(direct && outdeg)) {
+    GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
+    GX_CUDA(cudaMemcpy(e->d_outdeg, e->outdeg.data(), sizeof(int32_t) * V, cudaMemcpyHostToDevice));
+  }
   for (int i = 0; i < 2; ++i) {
     uint32_t* vp = nullptr;
     GX_TRY(dev_alloc(&vp, static_cast<size_t>(V)));
@@ -946,8 +1112,23 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   e->n_work = kQueues * (P + 2);
   GX_TRY(dev_alloc(&e->d_work, static_cast<size_t>(e->n_work)));
   phase("vertex arrays");
-  GX_TRY(plan_shards(e, src_col));
-  {
+  if (direct) {
+    unsigned int h = 0;
+    cudaError_t err = cudaMemcpyAsync(&h, scratch.flag, sizeof(h), cudaMemcpyDeviceToHost, e->s_copy);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(e->s_copy);
+    if (err != cudaSuccess) return fail(GX_ERR_CUDA, "gx_load_csc upload: %s", cudaGetErrorString(err));
+    phase("uploaded");
+    if (h & 1u) {
+      e->release_graph();
+      return fail(GX_ERR_INVALID, "gx_load_csc: off is not non-decreasing");
+    }
+    if (h & 2u) {
+      e->release_graph();
+      return fail(GX_ERR_INVALID, "gx_load_csc: source id outside [0, %d)", V);
+    }
+  }
+  GX_TRY(plan_shards(e, src_col, direct));
+  if (!direct) {
     // Offsets non-decreasing, and (fully resident) every source id in range.
     unsigned int* flag = nullptr;
     GX_TRY(dev_alloc(&flag, 1));
@@ -969,7 +1150,7 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
     }
   }
   phase("edges");
-  GX_TRY(build_signatures(e));
+  if (!direct) GX_TRY(build_signatures(e));
   phase("signatures");
   if (e->all_resident) {
     if (e->cfg.layout == 1) GX_TRY(build_blocks(e, src_col));
@@ -996,6 +1177,22 @@ gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
   if (!e->loaded) return fail(GX_ERR_STATE, "gx_set_weights: no graph loaded");
   GX_CUDA(cudaSetDevice(e->dev));
   if (!e->all_resident && !e->h_col) return fail(GX_ERR_STATE, "gx_set_weights: streaming source missing");
+  if (e->all_resident && e->cfg.cache_budget_bytes < 0) {
+    // No budget: the weights go straight to the device.
+    e->has_weights = true;
+    GX_TRY(dev_alloc(&e->d_w, static_cast<size_t>(e->E) + 8));
+    GX_CUDA(cudaMemsetAsync(e->d_w + e->E, 0, 8 * sizeof(uint32_t), e->s_copy));
+    GX_TRY(upload_async(e, e->d_w, w, sizeof(uint32_t) * static_cast<size_t>(e->E), e->s_copy));
+    GX_CUDA(cudaStreamSynchronize(e->s_copy));
+    if (e->blocks_ready) {
+      std::vector<uint32_t> wp(static_cast<size_t>(e->b_edges) + 4, 0u);
+      fill_block_layout<uint32_t>(e, w, wp.data());
+      GX_TRY(dev_alloc(&e->d_wp, wp.size()));
+      GX_CUDA(cudaMemcpy(e->d_wp, wp.data(), sizeof(uint32_t) * wp.size(), cudaMemcpyHostToDevice));
+    }
+    e->out_built = false;
+    return GX_OK;
+  }
   if (e->h_w) cudaFreeHost(e->h_w);
   e->h_w = nullptr;
   GX_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->h_w), (e->E + 8) * sizeof(uint32_t), cudaHostAllocDefault));
@@ -1009,7 +1206,7 @@ gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
       // Need the column data on the host again to re-plan.
       GX_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->h_col), (e->E + 8) * sizeof(int32_t), cudaHostAllocDefault));
       GX_CUDA(cudaMemcpy(e->h_col, e->d_col, (e->E + 8) * sizeof(int32_t), cudaMemcpyDeviceToHost));
-      GX_TRY(plan_shards(e, e->h_col));
+      GX_TRY(plan_shards(e, e->h_col, false));
       GX_TRY(build_signatures(e));
       if (e->all_resident) {
         cudaFreeHost(e->h_col);
@@ -1021,7 +1218,7 @@ gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
       GX_CUDA(cudaMemcpy(e->d_w, w, e->E * sizeof(uint32_t), cudaMemcpyHostToDevice));
     }
   } else {
-    GX_TRY(plan_shards(e, e->h_col));
+    GX_TRY(plan_shards(e, e->h_col, false));
   }
   if (e->all_resident && e->blocks_ready) {
     std::vector<uint32_t> wp(static_cast<size_t>(e->b_edges) + 4, 0u);

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 
 #include <cstring>
+#include <memory>
+#include <utility>
 #include <vector>
 
 #include "gx_internal.h"
@@ -26,27 +28,82 @@
 
 namespace gx {
 
+// Device memory of the engines comes from one stream-ordered pool per device
+// that keeps freed blocks (release threshold: unlimited), so loading a graph
+// after another engine was destroyed maps no new memory and destroying an
+// engine unmaps none.  gx_release_cached_memory() trims the pool.  Blocks are
+// handed out and returned on a private stream that is synchronised after each
+// call; callers free only memory no running kernel uses.
+struct DevicePool {
+  cudaMemPool_t pool = nullptr;
+  cudaStream_t stream = nullptr;
+};
+DevicePool* device_pool(int dev);  // nullptr if the device has no pool support
+int current_device();
+
+inline cudaError_t pool_malloc(void** p, size_t bytes) {
+  DevicePool* dp = device_pool(current_device());
+  if (!dp) return cudaMalloc(p, bytes);
+  cudaError_t err = cudaMallocFromPoolAsync(p, bytes, dp->pool, dp->stream);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(dp->stream);
+  return err;
+}
+
+inline void pool_free(void* p) {
+  if (!p) return;
+  DevicePool* dp = device_pool(current_device());
+  if (!dp) {
+    cudaFree(p);
+    return;
+  }
+  cudaFreeAsync(p, dp->stream);
+  cudaStreamSynchronize(dp->stream);
+}
+
 template <class T>
 gx_status dev_alloc(T** p, size_t n) {
   if (*p) {
-    cudaFree(*p);
+    pool_free(*p);
     *p = nullptr;
   }
   if (n == 0) n = 1;
-  cudaError_t err = cudaMalloc(reinterpret_cast<void**>(p), n * sizeof(T));
+  cudaError_t err = pool_malloc(reinterpret_cast<void**>(p), n * sizeof(T));
   if (err != cudaSuccess) {
     *p = nullptr;
     cudaGetLastError();
-    return fail(GX_ERR_OOM, "cudaMalloc of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(err));
+    return fail(GX_ERR_OOM, "device allocation of %zu bytes failed: %s", n * sizeof(T), cudaGetErrorString(err));
   }
   return GX_OK;
 }
 
 template <class T>
 void dev_free(T** p) {
-  if (*p) cudaFree(*p);
+  if (*p) pool_free(*p);
   *p = nullptr;
 }
+
+// std::vector storage without value-initialisation: large host arrays are
+// filled by parallel loops, which also place their pages.
+template <class T>
+struct UninitAlloc : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = UninitAlloc<U>;
+  };
+  UninitAlloc() = default;
+  template <class U>
+  UninitAlloc(const UninitAlloc<U>&) noexcept {}
+  template <class U>
+  void construct(U* ptr) noexcept {
+    ::new (static_cast<void*>(ptr)) U;
+  }
+  template <class U, class... A>
+  void construct(U* ptr, A&&... args) {
+    ::new (static_cast<void*>(ptr)) U(std::forward<A>(args)...);
+  }
+};
+template <class T>
+using hvec = std::vector<T, UninitAlloc<T>>;
 
 inline int app_kind(const gx_run_params& p) {
   switch (p.app) {
@@ -66,6 +123,7 @@ struct gx_engine {
   int dev = 0;
   int n_sm = 0;
   cudaStream_t s_comp = nullptr, s_copy = nullptr;
+  int pageable_access = 0;           // the device reads pageable host memory (cudaDevAttrPageableMemoryAccess)
   std::vector<cudaStream_t> s_copies;  // s_copy first
   bool loaded = false;
 
@@ -73,11 +131,11 @@ struct gx_engine {
   int32_t V = 0, P = 0;
   int64_t E = 0;
   std::vector<int32_t> bounds;
-  std::vector<int64_t> off;
-  std::vector<int32_t> outdeg;
+  gx::hvec<int64_t> off;
+  gx::hvec<int32_t> outdeg;
   int64_t n_dangling = 0;            // vertices of out-degree 0
-  std::vector<int2> units;
-  std::vector<int32_t> unit_shard;
+  gx::hvec<int2> units;
+  gx::hvec<int32_t> unit_shard;
   std::vector<int32_t> unit_begin;  // P+1
   std::vector<int4> heavy;
   int64_t n_partials = 0;
@@ -156,6 +214,9 @@ struct gx_engine {
   ~gx_engine() { release(); }
 
   void release_graph() {
+    // Pool frees do not wait for the device: let this engine's work finish.
+    if (s_comp) cudaStreamSynchronize(s_comp);
+    for (cudaStream_t cs : s_copies) cudaStreamSynchronize(cs);
     gx::dev_free(&d_off);
     gx::dev_free(&d_col);
     gx::dev_free(&d_w);

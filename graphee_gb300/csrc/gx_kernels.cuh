@@ -842,7 +842,7 @@ static __global__ void signature_kernel(unsigned long long* sig, const int32_t* 
 // The same masks for a fully resident graph in one launch: edge k belongs
 // to the shard whose edge range [ebound[p], ebound[p+1]) holds it.
 static __global__ void signature_all_kernel(unsigned long long* sig, const int32_t* col, const int64_t* ebound,
-                                            int32_t P, int32_t group) {
+                                            int32_t P, int32_t group, int32_t V) {
   const int64_t E = ebound[P];
   for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < E;
        k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
@@ -854,6 +854,8 @@ static __global__ void signature_all_kernel(unsigned long long* sig, const int32
     }
     const unsigned long long bit = 1ull << (lo / group);
     const int u = col[k];
+    // May run before the host has read the load-time checks: skip bad ids.
+    if (u < 0 || u >= V) continue;
     if ((sig[u] & bit) == 0) atomicOr(sig + u, bit);
   }
 }

@@ -130,6 +130,11 @@ const char* gx_last_error(void);
 gx_status gx_create(const gx_config* cfg, gx_engine** out);
 gx_status gx_destroy(gx_engine* e);
 
+/* Engines draw device memory from a per-device pool that keeps blocks after
+ * gx_destroy, so the next engine's load maps no new memory.  This returns
+ * the cached blocks of `device` to the driver.  No reference counterpart. */
+gx_status gx_release_cached_memory(int32_t device);
+
 /* Loads the reference's shard directory: {p}.edge.npy for p in [0,P), each a
  * 1-D int32 .npy of [E_p, len(indices), len(indptr), start, end, indices...,
  * indptr...] (GraphMP/system/Comp.h:33-42, written by
