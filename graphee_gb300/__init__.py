@@ -50,7 +50,9 @@ class Config(C.Structure):
 
 class RunParams(C.Structure):
     _fields_ = [("app", C.c_int), ("max_iter", C.c_int32), ("damping", C.c_double), ("source", C.c_int32),
-                ("weighted", C.c_int32), ("tolerance", C.c_double), ("use_init", C.c_int32)]
+                ("weighted", C.c_int32), ("tolerance", C.c_double), ("use_init", C.c_int32),
+                ("first_step", C.c_int32), ("async_mode", C.c_int32), ("checkpoint_every", C.c_int32),
+                ("checkpoint_prefix", C.c_char_p)]
 
 
 class RunStats(C.Structure):
@@ -108,6 +110,8 @@ def lib() -> C.CDLL:
         "gx_create": (C.c_int, [P, P]),
         "gx_destroy": (C.c_int, [P]),
         "gx_release_cached_memory": (C.c_int, [I32]),
+        "gx_write_values_npy": (C.c_int, [P, C.c_char_p]),
+        "gx_read_values_npy": (C.c_int, [C.c_char_p, I64, P]),
         "gx_load_shards": (C.c_int, [P, C.c_char_p, I32, I32]),
         "gx_load_csc": (C.c_int, [P, I32, I32, P, P, P, P]),
         "gx_set_weights": (C.c_int, [P, P]),
@@ -300,6 +304,13 @@ def batch_graph(n: int, scales=(10, 17), edge_factors=(8, 32), seed: int = 1, a=
 
 # ---------------------------------------------------------------- engine ----
 
+def read_values(path: str, n: int) -> np.ndarray:
+    """A checkpoint written by Engine.write_values or gx_run (4-byte elements)."""
+    out = np.empty(n, np.uint32)
+    _check(lib().gx_read_values_npy(str(path).encode(), n, _ptr(out)), "gx_read_values_npy")
+    return out
+
+
 def release_cached_memory(device: int = 0) -> None:
     """Returns the device memory engines keep cached after close()."""
     _check(lib().gx_release_cached_memory(device), "gx_release_cached_memory")
@@ -367,7 +378,7 @@ class Engine:
         _check(lib().gx_set_init(self._h, _ptr(vals)), "gx_set_init")
 
     def run(self, app: int, max_iter: int, damping=0.85, source=None, weighted=False, tolerance=0.0,
-            use_init=False) -> dict:
+            use_init=False, first_step=0, async_mode=False, checkpoint_every=0, checkpoint_prefix=None) -> dict:
         p = RunParams()
         lib().gx_run_params_default(C.byref(p), app)
         p.max_iter = max_iter
@@ -377,6 +388,11 @@ class Engine:
         p.weighted = int(weighted)
         p.tolerance = tolerance
         p.use_init = int(use_init)
+        p.first_step = first_step
+        p.async_mode = int(async_mode)
+        p.checkpoint_every = checkpoint_every
+        prefix = None if checkpoint_prefix is None else str(checkpoint_prefix).encode()
+        p.checkpoint_prefix = prefix
         st = RunStats()
         _check(lib().gx_run(self._h, C.byref(p), C.byref(st)), "gx_run")
         self.app = app
@@ -452,6 +468,10 @@ class Engine:
                "gx_pagerank_warm")
         self.app = APP_PAGERANK_STD
         return ws.as_dict()
+
+    def write_values(self, path: str) -> None:
+        """Checkpoint: the current values as a 1-D .npy file."""
+        _check(lib().gx_write_values_npy(self._h, str(path).encode()), "gx_write_values_npy")
 
     def iter_stats(self, step: int) -> dict:
         s = IterStats()

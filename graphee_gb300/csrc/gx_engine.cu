@@ -527,6 +527,9 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
     GX_TRY(dev_alloc(&e->d_stats, static_cast<size_t>(std::max(prm.max_iter, 1))));
     e->stats_cap = prm.max_iter;
   }
+  // A resumed run has no statistics for the steps before first_step.
+  if (prm.first_step > 0)
+    GX_CUDA(cudaMemsetAsync(e->d_stats, 0, sizeof(StepStats) * prm.first_step, e->s_comp));
 
   // Control block.
   Ctl c{};
@@ -542,7 +545,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   c.fx_scale = static_cast<double>(V) * 1073741824.0;  // 2^30 per 1/N of rank
   c.tolerance = prm.tolerance;
   c.sel_threshold = e->cfg.selective_threshold;
-  c.step = 0;
+  c.step = prm.first_step;
+  c.async_mode = (min_app && prm.async_mode) ? 1 : 0;
   c.cur = 0;
   c.mode = MODE_DENSE;
   c.done = prm.max_iter <= 0;
@@ -639,10 +643,13 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   fa.n_work_ctr = e->n_work;
 
   void (*pull)(PullArgs) = e->cfg.exact_order ? pull_kernel<APP, true> : pull_kernel<APP, false>;
+  if constexpr (APP == K_SSSP_UNIT || APP == K_SSSP_W || APP == K_CC) {
+    if (c.async_mode) pull = pull_kernel<APP, false, true>;
+  }
   const int grid_pull = occupancy_grid<APP>(e, reinterpret_cast<const void*>(pull));
   // Block layout (config.layout = 1): the TMA-staged block kernel.
   const bool use_blocks = e->cfg.layout == 1 && e->all_resident && e->blocks_ready && !e->cfg.exact_order &&
-                          APP != K_INDEG &&
+                          APP != K_INDEG && !c.async_mode &&
                           (APP != K_SSSP_W || e->d_wp != nullptr);
   BlockArgs ba{};
   int grid_block = 0;
@@ -679,6 +686,22 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   GX_CUDA(cudaEventCreate(&ev1));
   std::unique_ptr<cudaEvent_t, void (*)(cudaEvent_t*)> g0(&ev0, [](cudaEvent_t* x) { cudaEventDestroy(*x); });
   std::unique_ptr<cudaEvent_t, void (*)(cudaEvent_t*)> g1(&ev1, [](cudaEvent_t* x) { cudaEventDestroy(*x); });
+  // Checkpoints: the values after every checkpoint_every supersteps, written
+  // at the host's sync points ({prefix}{step}.npy).
+  const int every = prm.checkpoint_every > 0 ? prm.checkpoint_every : 0;
+  int32_t last_ckpt = prm.first_step;
+  std::vector<uint32_t> ckpt_buf;
+  auto checkpoint = [&](const Ctl& hc) -> gx_status {
+    if (!every || hc.step == last_ckpt || hc.step % every != 0) return GX_OK;
+    ckpt_buf.resize(static_cast<size_t>(V));
+    GX_CUDA(cudaMemcpy(ckpt_buf.data(), hc.cur ? e->d_val[1] : e->d_val[0], sizeof(uint32_t) * V,
+                       cudaMemcpyDeviceToHost));
+    const std::string path = std::string(prm.checkpoint_prefix) + std::to_string(hc.step) + ".npy";
+    const char* descr = is_pr<APP>() ? "<f4" : (APP == K_SSSP_W ? "<u4" : "<i4");
+    if (!write_npy_4(path, ckpt_buf.data(), V, descr)) return fail(GX_ERR_IO, "cannot write checkpoint %s", path.c_str());
+    last_ckpt = hc.step;
+    return GX_OK;
+  };
   int64_t h2d_bytes = 0;
   int32_t streamed = 0;
   int32_t launches = 1;  // init_kernel
@@ -690,7 +713,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   if (e->all_resident) {
     // Replay K supersteps per CUDA graph launch; the control block makes
     // steps after termination no-ops.
-    const int K = std::max(1, std::min(prm.max_iter, 8));
+    // Checkpointing syncs after every superstep, so it launches directly.
+    const int K = every ? 1 : std::max(1, std::min(prm.max_iter - prm.first_step, 8));
     const bool prof = e->cfg.profile != 0;
     std::vector<cudaEvent_t> pev(prof ? 2 * K : 0);
     for (auto& ev : pev) GX_CUDA(cudaEventCreate(&ev));
@@ -712,7 +736,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
     cudaGraphExec_t exec = nullptr;
     // Profiling times each pull launch with its own events, so it launches
     // directly instead of replaying a graph.
-    if (e->cfg.use_graph && !prof) {
+    if (e->cfg.use_graph && !prof && !every) {
       cudaGraph_t graph;
       GX_CUDA(cudaStreamBeginCapture(e->s_comp, cudaStreamCaptureModeThreadLocal));
       for (int i = 0; i < K; ++i) {
@@ -729,8 +753,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
       launches = 0;
     }
     const int per_step = push_ok ? 3 : 2;
-    int steps_before = 0;
-    for (int launched = 0; launched < prm.max_iter; launched += K) {
+    int steps_before = prm.first_step;
+    for (int launched = prm.first_step; launched < prm.max_iter; launched += K) {
       if (exec) {
         GX_CUDA(cudaGraphLaunch(exec, e->s_comp));
         launches += K * per_step;
@@ -751,6 +775,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
       }
       pull_launches += ran;
       steps_before = e->h_ctl->step;
+      GX_TRY(checkpoint(*e->h_ctl));
       if (e->h_ctl->done) break;
     }
     if (exec) cudaGraphExecDestroy(exec);
@@ -764,10 +789,11 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
     GX_CUDA(cudaEventCreate(&k0));
     GX_CUDA(cudaEventCreate(&k1));
     int slot = 0;
-    for (int step = 0; step < prm.max_iter; ++step) {
+    for (int step = prm.first_step; step < prm.max_iter; ++step) {
       GX_CUDA(cudaMemcpyAsync(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->s_comp));
       GX_CUDA(cudaStreamSynchronize(e->s_comp));
       const Ctl& hc = *e->h_ctl;
+      GX_TRY(checkpoint(hc));
       if (hc.done) break;
       const bool sel = hc.mode == MODE_SELECTIVE;
       GX_CUDA(cudaEventRecord(k0, e->s_comp));
@@ -842,6 +868,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   GX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
 
   if (e->h_ctl->error == 2) return fail(GX_ERR_CUDA, "gx_run: push frontier overflow");
+  GX_TRY(checkpoint(*e->h_ctl));
   const int32_t steps = e->h_ctl->step;
   e->last_steps = steps;
   e->last_stats.assign(std::max(steps, 0), StepStats{});
@@ -872,6 +899,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   }
   e->last_run = rs;
   e->last_app = prm.app;
+  e->last_weighted = APP == K_SSSP_W;
   if (out) *out = rs;
   return GX_OK;
 }
@@ -908,6 +936,10 @@ void gx_run_params_default(gx_run_params* p, gx_app app) {
   p->weighted = 0;
   p->tolerance = 0;
   p->use_init = 0;
+  p->first_step = 0;
+  p->async_mode = 0;
+  p->checkpoint_every = 0;
+  p->checkpoint_prefix = nullptr;
 }
 
 gx_status gx_create(const gx_config* cfg, gx_engine** out) {
@@ -1252,6 +1284,14 @@ gx_status gx_run(gx_engine* e, const gx_run_params* prm, gx_run_stats* stats) {
   if (prm->app == GX_APP_SSSP && (prm->source < 0 || prm->source >= e->V))
     return fail(GX_ERR_INVALID, "gx_run: SSSP source %d outside [0, %d)", prm->source, e->V);
   if (kind == K_SSSP_W && !e->has_weights) return fail(GX_ERR_STATE, "gx_run: weighted SSSP needs gx_set_weights");
+  if (prm->first_step < 0 || (prm->max_iter > 0 && prm->first_step >= prm->max_iter))
+    return fail(GX_ERR_INVALID, "gx_run: first_step %d outside [0, max_iter=%d)", prm->first_step, prm->max_iter);
+  if (prm->first_step > 0 && !prm->use_init)
+    return fail(GX_ERR_INVALID, "gx_run: first_step > 0 resumes from gx_set_init values; set use_init");
+  if (prm->async_mode && !(kind == K_SSSP_UNIT || kind == K_SSSP_W || kind == K_CC))
+    return fail(GX_ERR_INVALID, "gx_run: async_mode is for SSSP and CC");
+  if (prm->checkpoint_every < 0 || (prm->checkpoint_every > 0 && !prm->checkpoint_prefix))
+    return fail(GX_ERR_INVALID, "gx_run: checkpoint_every needs checkpoint_prefix");
   GX_CUDA(cudaSetDevice(e->dev));
   gx_run_params p = *prm;
   if (p.max_iter == 0) {
@@ -1280,6 +1320,18 @@ gx_status gx_get_values(gx_engine* e, void* host_out) {
   GX_CUDA(cudaMemcpy(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
   const int cur = e->h_ctl->cur & 1;
   GX_CUDA(cudaMemcpy(host_out, e->d_val[cur], sizeof(uint32_t) * e->V, cudaMemcpyDeviceToHost));
+  return GX_OK;
+}
+
+gx_status gx_write_values_npy(gx_engine* e, const char* path) {
+  if (!e || !path) return fail(GX_ERR_INVALID, "gx_write_values_npy: bad arguments");
+  if (!e->loaded) return fail(GX_ERR_STATE, "gx_write_values_npy: no graph loaded");
+  std::vector<uint32_t> buf(static_cast<size_t>(e->V));
+  GX_TRY(gx_get_values(e, buf.data()));
+  const bool pr = e->last_app == GX_APP_PAGERANK_REF || e->last_app == GX_APP_PAGERANK_STD;
+  const bool wt = e->last_app == GX_APP_SSSP && e->last_weighted;
+  if (!write_npy_4(path, buf.data(), e->V, pr ? "<f4" : (wt ? "<u4" : "<i4")))
+    return fail(GX_ERR_IO, "cannot write %s", path);
   return GX_OK;
 }
 

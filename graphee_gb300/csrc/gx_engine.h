@@ -207,6 +207,7 @@ struct gx_engine {
 
   // last run
   gx_app last_app = GX_APP_PAGERANK_REF;
+  bool last_weighted = false;
   int32_t last_steps = 0;
   std::vector<gx::StepStats> last_stats;
   gx_run_stats last_run{};

@@ -65,11 +65,42 @@ void exclusive_scan(const int64_t* cnt, int64_t n, int64_t* out) {
   out[n] = part[nt];
 }
 
-// ---- .npy (format version 1.0, 1-D little-endian int32) ----
+// ---- .npy (format version 1.0, 1-D little-endian 4-byte elements) ----
 
 bool write_npy_i32(const std::string& path, const int32_t* data, int64_t n) {
+  return write_npy_4(path, data, n, "<i4");
+}
+
+// Opens a 1-D int32 .npy and leaves `f` positioned at the first element.
+gx_status open_npy_i32(const std::string& path, FILE** out, int64_t* n) {
+  char descr = 0;
+  gx_status st = open_npy_4(path, out, n, &descr);
+  if (st != GX_OK) return st;
+  if (descr != 'i') {
+    fclose(*out);
+    *out = nullptr;
+    return fail(GX_ERR_FORMAT, "%s: expected a 1-D little-endian int32 array", path.c_str());
+  }
+  return GX_OK;
+}
+
+gx_status read_npy_i32(const std::string& path, std::vector<int32_t>* v) {
+  FILE* f;
+  int64_t n;
+  gx_status st = open_npy_i32(path, &f, &n);
+  if (st != GX_OK) return st;
+  v->resize(static_cast<size_t>(n));
+  size_t got = n ? fread(v->data(), sizeof(int32_t), static_cast<size_t>(n), f) : 0;
+  fclose(f);
+  if (got != static_cast<size_t>(n)) return fail(GX_ERR_IO, "%s: short read", path.c_str());
+  return GX_OK;
+}
+
+}  // namespace
+
+bool write_npy_4(const std::string& path, const void* data, int64_t n, const char* descr) {
   char dict[160];
-  int dl = snprintf(dict, sizeof(dict), "{'descr': '<i4', 'fortran_order': False, 'shape': (%lld,), }",
+  int dl = snprintf(dict, sizeof(dict), "{'descr': '%s', 'fortran_order': False, 'shape': (%lld,), }", descr,
                     static_cast<long long>(n));
   int total = 10 + dl + 1;
   int pad = (64 - total % 64) % 64;
@@ -83,13 +114,14 @@ bool write_npy_i32(const std::string& path, const int32_t* data, int64_t n) {
   FILE* f = fopen(path.c_str(), "wb");
   if (!f) return false;
   bool ok = fwrite(hdr.data(), 1, hdr.size(), f) == hdr.size();
-  if (ok && n > 0) ok = fwrite(data, sizeof(int32_t), static_cast<size_t>(n), f) == static_cast<size_t>(n);
+  if (ok && n > 0) ok = fwrite(data, 4, static_cast<size_t>(n), f) == static_cast<size_t>(n);
   ok = (fclose(f) == 0) && ok;
   return ok;
 }
 
-// Opens a 1-D int32 .npy and leaves `f` positioned at the first element.
-gx_status open_npy_i32(const std::string& path, FILE** out, int64_t* n) {
+// Opens a 1-D little-endian .npy of 4-byte elements (int32, uint32 or
+// float32; `kind` gets 'i', 'u' or 'f') positioned at the first element.
+gx_status open_npy_4(const std::string& path, FILE** out, int64_t* n, char* kind) {
   FILE* f = fopen(path.c_str(), "rb");
   if (!f) return fail(GX_ERR_IO, "cannot open %s: %s", path.c_str(), strerror(errno));
   unsigned char pre[10];
@@ -113,13 +145,17 @@ gx_status open_npy_i32(const std::string& path, FILE** out, int64_t* n) {
     fclose(f);
     return fail(GX_ERR_FORMAT, "%s: short header", path.c_str());
   }
-  bool i4 = h.find("'<i4'") != std::string::npos || h.find("'|i4'") != std::string::npos;
+  char k = 0;
+  if (h.find("'<i4'") != std::string::npos || h.find("'|i4'") != std::string::npos) k = 'i';
+  else if (h.find("'<u4'") != std::string::npos || h.find("'|u4'") != std::string::npos) k = 'u';
+  else if (h.find("'<f4'") != std::string::npos) k = 'f';
   bool fortran = h.find("'fortran_order': True") != std::string::npos;
   size_t lp = h.find('('), rp = h.find(')');
-  if (!i4 || fortran || lp == std::string::npos || rp == std::string::npos) {
+  if (!k || fortran || lp == std::string::npos || rp == std::string::npos) {
     fclose(f);
-    return fail(GX_ERR_FORMAT, "%s: expected a 1-D little-endian int32 array", path.c_str());
+    return fail(GX_ERR_FORMAT, "%s: expected a 1-D little-endian array of 4-byte elements", path.c_str());
   }
+  *kind = k;
   std::string shape = h.substr(lp + 1, rp - lp - 1);
   if (std::count(shape.begin(), shape.end(), ',') > 1 ||
       (shape.find(',') != std::string::npos && shape.find_first_not_of(" ", shape.find(',') + 1) != std::string::npos)) {
@@ -131,24 +167,30 @@ gx_status open_npy_i32(const std::string& path, FILE** out, int64_t* n) {
   return GX_OK;
 }
 
-gx_status read_npy_i32(const std::string& path, std::vector<int32_t>* v) {
-  FILE* f;
-  int64_t n;
-  gx_status st = open_npy_i32(path, &f, &n);
-  if (st != GX_OK) return st;
-  v->resize(static_cast<size_t>(n));
-  size_t got = n ? fread(v->data(), sizeof(int32_t), static_cast<size_t>(n), f) : 0;
-  fclose(f);
-  if (got != static_cast<size_t>(n)) return fail(GX_ERR_IO, "%s: short read", path.c_str());
-  return GX_OK;
-}
-
-}  // namespace
 }  // namespace gx
 
 using namespace gx;
 
 extern "C" {
+
+gx_status gx_read_values_npy(const char* path, int64_t n, void* out) {
+  if (!path || n < 0 || (n > 0 && !out)) return fail(GX_ERR_INVALID, "gx_read_values_npy: bad arguments");
+  FILE* f = nullptr;
+  int64_t m = 0;
+  char kind = 0;
+  gx_status st = open_npy_4(path, &f, &m, &kind);
+  if (st != GX_OK) return st;
+  if (m != n) {
+    fclose(f);
+    return fail(GX_ERR_FORMAT, "%s: %lld elements, expected %lld", path, static_cast<long long>(m),
+                static_cast<long long>(n));
+  }
+  const bool ok = n == 0 || fread(out, 4, static_cast<size_t>(n), f) == static_cast<size_t>(n);
+  fclose(f);
+  if (!ok) return fail(GX_ERR_FORMAT, "%s: short data", path);
+  return GX_OK;
+}
+
 
 const char* gx_last_error(void) { return g_last_error.c_str(); }
 

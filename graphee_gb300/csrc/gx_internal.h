@@ -12,6 +12,12 @@ namespace gx {
 // Records `msg` as the thread's last error and returns `st`.
 gx_status fail(gx_status st, const char* fmt, ...);
 
+// 1-D little-endian .npy files of 4-byte elements (descr "<i4", "<u4" or
+// "<f4").  open_npy_4 leaves `*out` at the first element and sets `*kind` to
+// 'i', 'u' or 'f'.
+bool write_npy_4(const std::string& path, const void* data, int64_t n, const char* descr);
+gx_status open_npy_4(const std::string& path, FILE** out, int64_t* n, char* kind);
+
 // splitmix64 finaliser (Steele, Lea, Flood, "Fast splittable pseudorandom
 // number generators", OOPSLA 2014): a bijective 64-bit mixer used as a
 // counter-based generator, so any element can be produced independently.

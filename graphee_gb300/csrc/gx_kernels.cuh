@@ -44,6 +44,8 @@ struct Ctl {
   int shard_group;          // shards per bit of the 64-bit shard mask
   int push_ok;              // out-edges resident: sparse steps may push
   int step0_push;           // SSSP from init_vertex: step 0 pushes from the source alone
+  int async_mode;           // min apps: pull updates values in place (no buffer swap)
+  int pad0;
   unsigned long long push_edge_limit;  // push when the frontier has at most this many out-edges
   double damping;
   double inv_n;             // 1.0 / N, as the reference computes it
@@ -132,18 +134,27 @@ __device__ __forceinline__ uint32_t sat_add(uint32_t a, uint32_t b) {
 #define GX_GATHER_CG 0
 #endif
 
-template <int APP>
+// ASYNC (Gauss-Seidel, min apps only): values are read and written in one
+// buffer during the step, so gathers go through L2 (ld.cg), never the
+// read-only path.
+template <class T, bool ASYNC>
+__device__ __forceinline__ T ld_val(const T* p) {
+  if constexpr (ASYNC) return __ldcg(p);
+  else return __ldg(p);
+}
+
+template <int APP, bool ASYNC = false>
 __device__ __forceinline__ typename AppTraits<APP>::T edge_value(const PullArgs& a, const void* src_val,
                                                                  const float* src_con, int32_t u, uint32_t wt) {
   if constexpr (is_pr<APP>()) {
     if (GX_GATHER_CG) return __ldcg(src_con + u);
     return __ldg(src_con + u);
   } else if constexpr (APP == K_SSSP_UNIT) {
-    return __ldg(static_cast<const int32_t*>(src_val) + u) + 1;  // sssp.cpp:43
+    return ld_val<int32_t, ASYNC>(static_cast<const int32_t*>(src_val) + u) + 1;  // sssp.cpp:43
   } else if constexpr (APP == K_SSSP_W) {
-    return sat_add(__ldg(static_cast<const uint32_t*>(src_val) + u), wt);
+    return sat_add(ld_val<uint32_t, ASYNC>(static_cast<const uint32_t*>(src_val) + u), wt);
   } else {
-    return __ldg(static_cast<const int32_t*>(src_val) + u);      // cc.cpp:42
+    return ld_val<int32_t, ASYNC>(static_cast<const int32_t*>(src_val) + u);      // cc.cpp:42
   }
 }
 
@@ -295,7 +306,7 @@ __device__ __forceinline__ void flush_block(Ctl* ctl, const LocalAcc& la) {
 // Warp-cooperative reduction of the edge range [b, e) (all lanes call it with
 // the same range): lanes take 8 consecutive edges each per round, with
 // 128-bit loads; the per-lane partials are combined by a fixed xor tree.
-template <int APP>
+template <int APP, bool ASYNC = false>
 __device__ __forceinline__ typename AppTraits<APP>::T warp_reduce_range(const PullArgs& a, const void* src_val,
                                                                         const float* src_con, int64_t b, int64_t e,
                                                                         int lane) {
@@ -317,7 +328,7 @@ __device__ __forceinline__ typename AppTraits<APP>::T warp_reduce_range(const Pu
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int64_t k = (j < 4 ? q : q2) + (j & 3);
-      vals[j] = (k >= b && k < e) ? edge_value<APP>(a, src_val, src_con, cs[j], ws[j]) : identity<APP>();
+      vals[j] = (k >= b && k < e) ? edge_value<APP, ASYNC>(a, src_val, src_con, cs[j], ws[j]) : identity<APP>();
     }
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc = combine<APP>(acc, vals[j]);
@@ -331,7 +342,7 @@ __device__ __forceinline__ typename AppTraits<APP>::T warp_reduce_range(const Pu
 #define GX_PULL_MIN_BLOCKS 4
 #endif
 
-template <int APP, bool EXACT>
+template <int APP, bool EXACT, bool ASYNC = false>
 __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(PullArgs a) {
   typedef typename AppTraits<APP>::T T;
   __shared__ __align__(16) T s_buf[EXACT ? kWarps : 1][EXACT ? kChunk : 4];
@@ -351,7 +362,8 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
   // Ternaries, not a[cur]: indexing a parameter array with a runtime value
   // would copy the whole parameter block to local memory.
   const void* src_val = cur ? a.val[1] : a.val[0];
-  void* dst_val = cur ? a.val[0] : a.val[1];
+  // Gauss-Seidel: new values overwrite the current ones in place.
+  void* dst_val = ASYNC ? const_cast<void*>(src_val) : (cur ? a.val[0] : a.val[1]);
   const float* src_con = cur ? a.con[1] : a.con[0];
   float* dst_con = cur ? a.con[0] : a.con[1];
   const bool selective = mode == MODE_SELECTIVE;
@@ -396,7 +408,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
         const int pv = px + lane;
         pbeg = a.off[pv];
         pend = a.off[pv + 1];
-        pold = __ldcs(static_cast<const T*>(src_val) + pv);
+        pold = ASYNC ? __ldcg(static_cast<const T*>(src_val) + pv) : __ldcs(static_cast<const T*>(src_val) + pv);
         if constexpr (is_pr<APP>()) pod = __ldcs(a.outdeg + pv);
       }
     };
@@ -424,7 +436,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
         const int64_t b = vb + static_cast<int64_t>(wu.y) * kHeavyChunk;
         const int64_t e = ve < b + kHeavyChunk ? ve : b + kHeavyChunk;
         T acc = identity<APP>();
-        if constexpr (APP != K_INDEG) acc = warp_reduce_range<APP>(a, src_val, src_con, b, e, lane);
+        if constexpr (APP != K_INDEG) acc = warp_reduce_range<APP, ASYNC>(a, src_val, src_con, b, e, lane);
         if (lane == 0) {
           la.edges += e - b;
           T* part = static_cast<T*>(a.partial);
@@ -470,7 +482,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
       } else if (lane < n) {
         beg = a.off[v];
         end = a.off[v + 1];
-        old = __ldcs(static_cast<const T*>(src_val) + v);
+        old = ASYNC ? __ldcg(static_cast<const T*>(src_val) + v) : __ldcs(static_cast<const T*>(src_val) + v);
         if constexpr (is_pr<APP>()) od = __ldcs(a.outdeg + v);
       }
       // Vertices above the heavy threshold are applied by their own units.
@@ -508,7 +520,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                   const int64_t kk = q + e;
-                  x[e] = (kk >= E0 && kk < E1) ? edge_value<APP>(a, src_val, src_con, cs[e], ws[e]) : identity<APP>();
+                  x[e] = (kk >= E0 && kk < E1) ? edge_value<APP, ASYNC>(a, src_val, src_con, cs[e], ws[e]) : identity<APP>();
                 }
                 store4(buf + 4 * (lane + 32 * j), x);
               }
@@ -553,7 +565,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
 #pragma unroll
               for (int j = 0; j < 8; ++j) {
                 const int64_t kk = k + j;
-                vals[j] = (kk >= beg && kk < lend) ? edge_value<APP>(a, src_val, src_con, cs[j], ws[j])
+                vals[j] = (kk >= beg && kk < lend) ? edge_value<APP, ASYNC>(a, src_val, src_con, cs[j], ws[j])
                                                    : identity<APP>();
               }
 #pragma unroll
@@ -569,7 +581,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
             const int l = __ffs(m) - 1;
             const int64_t bl = __shfl_sync(0xffffffffu, beg, l);
             const int64_t el = __shfl_sync(0xffffffffu, end, l);
-            const T r = warp_reduce_range<APP>(a, src_val, src_con, bl, el, lane);
+            const T r = warp_reduce_range<APP, ASYNC>(a, src_val, src_con, bl, el, lane);
             if (lane == l) acc = combine<APP>(acc, r);
           }
         }
@@ -699,7 +711,7 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
   // are few enough to beat a full pull.
   const bool push_next = c.push_ok && (sel_next || c.front_edges <= c.push_edge_limit);
   const bool want_mask = sel_next && !push_next && a.sig != nullptr;
-  const int nb = c.mode == MODE_PUSH ? c.cur : (c.cur ^ 1);
+  const int nb = (c.mode == MODE_PUSH || c.async_mode) ? c.cur : (c.cur ^ 1);
   const T* newv = static_cast<const T*>(nb ? a.val[1] : a.val[0]);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   unsigned long long act = 0, mask = 0;
@@ -784,7 +796,7 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
     const double resid = static_cast<double>(s.resid_fx) / c.fx_scale;
     int done = (s.changed == 0 && c.step > 1) || (c.step + 1 >= c.max_iter);  // GraphPS.h:256,383
     if (is_pr<APP>() && c.tolerance > 0 && resid < c.tolerance) done = 1;
-    ctl->cur = c.mode == MODE_PUSH ? c.cur : (c.cur ^ 1);  // Msg <- MsgNew as a swap
+    ctl->cur = nb;  // Msg <- MsgNew as a swap (in place: push steps, async mode)
     ctl->mode = push_next ? MODE_PUSH : (sel_next ? MODE_SELECTIVE : MODE_DENSE);
     ctl->shard_mask = want_mask ? next_mask : ~0ull;
     ctl->shard_mask_next = 0;

@@ -91,6 +91,14 @@ typedef struct gx_run_params {
   int32_t weighted;      /* SSSP: 1 = weights from gx_set_weights, 0 = unit weight */
   double tolerance;      /* PageRank: also stop once the L1 residual < tolerance (0 = off) */
   int32_t use_init;      /* 1 = start from gx_set_init values instead of the app's init_vertex */
+  int32_t first_step;    /* resume: number the first superstep this (use_init must be set; the
+                            step counter, the step-0 comparison against 0 and the stop rule
+                            then continue as in the interrupted run; default 0) */
+  int32_t async_mode;    /* SSSP/CC: 1 = Gauss-Seidel supersteps that update values in place, as
+                            GraphH's USE_ASYNC; same final values, fewer supersteps, per-step
+                            counts differ from the reference's Jacobi loop (default 0) */
+  int32_t checkpoint_every;        /* write the values every this many supersteps (0 = off) */
+  const char* checkpoint_prefix;   /* ... to {prefix}{step}.npy, step = supersteps completed */
 } gx_run_params;
 
 typedef struct gx_run_stats {
@@ -161,6 +169,15 @@ gx_status gx_run(gx_engine* e, const gx_run_params* params, gx_run_stats* stats)
 
 /* Copies the final _VertexMsg (T[V]) to host memory. */
 gx_status gx_get_values(gx_engine* e, void* host_out);
+
+/* Checkpoint/resume of vertex state.  gx_write_values_npy writes the current
+ * values as a 1-D .npy ('<f4' PageRank, '<u4' weighted SSSP, '<i4' otherwise);
+ * gx_read_values_npy reads such a file of exactly n elements into `out`, to be
+ * passed to gx_set_init and resumed with params.use_init and params.first_step.
+ * gx_run also writes them every params.checkpoint_every supersteps.  The
+ * reference has no checkpoints (GraphPS.h keeps vertex state in memory only). */
+gx_status gx_write_values_npy(gx_engine* e, const char* path);
+gx_status gx_read_values_npy(const char* path, int64_t n, void* out);
 
 /* Per-step statistics of the last gx_run (the reference logs these per
  * iteration, GraphPS.h:375-382). */

@@ -128,3 +128,21 @@ def test_convert_edge_list(tmp_path):
     with pytest.raises(gx.GxError) as ei:
         gx.convert_edge_list(tmp_path / "bad.tsv", 1024, 2, tmp_path / "t")
     assert ei.value.status == gx.GX_ERR_FORMAT
+
+
+def test_values_npy_roundtrip_and_errors(tmp_path):
+    for dt in (np.float32, np.int32, np.uint32):
+        a = (np.arange(1000) * 7 % 113).astype(dt)
+        p = tmp_path / f"v_{np.dtype(dt).str[1:]}.npy"
+        np.save(p, a)
+        back = gx.read_values(p, a.size)
+        assert np.array_equal(back.view(dt), a)
+    p = tmp_path / "v.npy"
+    np.save(p, np.zeros(10, np.float32))
+    with pytest.raises(gx.GxError):
+        gx.read_values(p, 11)                       # wrong length
+    np.save(tmp_path / "d.npy", np.zeros(10, np.float64))
+    with pytest.raises(gx.GxError):
+        gx.read_values(tmp_path / "d.npy", 10)      # 8-byte elements
+    with pytest.raises(gx.GxError):
+        gx.read_values(tmp_path / "missing.npy", 10)
