@@ -152,10 +152,13 @@ def ncu_traffic(workload: str):
     return None
 
 
-def build_graph(args):
+def build_graph(args, device=None):
+    """The R-MAT graph: built on GPU `device` (gx_rmat_csc_gpu), or on the
+    host when device is None; both give the same graph."""
     import graphee_gb300 as gx
     t0 = time.time()
-    g = gx.rmat_graph(args.scale, args.edge_factor, seed=SEED, P=SHARDS)
+    g = gx.rmat_graph(args.scale, args.edge_factor, seed=SEED, P=SHARDS, gpu=device is not None,
+                      device=device or 0)
     return g, time.time() - t0
 
 
@@ -223,7 +226,7 @@ def run_gx(args, rank, local_rank, world):
             dist.barrier()
         torch.cuda.synchronize()
 
-    g, build_s = build_graph(args)
+    g, build_s = build_graph(args, device=local_rank)
     eng = gx.Engine(device=local_rank)
     eng.load(g)
     for _ in range(args.warmup):
@@ -306,7 +309,8 @@ def run_gx(args, rank, local_rank, world):
 
     if rank == 0:
         cfg = base_config(args, g)
-        cfg.update({"parallelism": f"replicas{world}", "graph_build_s": round(build_s, 2)})
+        cfg.update({"parallelism": f"replicas{world}", "graph_build_s": round(build_s, 2),
+                    "graph_build": "on the GPU (gx_rmat_csc_gpu), identical to the host build"})
         line = {"metric": "pagerank_gteps", "value": value, "unit": "GTEPS", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded R-MAT)",
@@ -346,7 +350,7 @@ def run_cc_tc(args):
     sys.path.insert(0, str(ROOT / "oracle"))
     import gx_oracle as O
     t0 = time.time()
-    g = gx.rmat_graph(args.scale, args.edge_factor, seed=SEED, P=SHARDS, symmetric=True)
+    g = gx.rmat_graph(args.scale, args.edge_factor, seed=SEED, P=SHARDS, symmetric=True, gpu=True)
     build_s = time.time() - t0
     with gx.Engine() as e:
         e.load(g)
@@ -376,7 +380,7 @@ def run_stream(args):
     import graphee_gb300 as gx
     scale = args.scale if args.scale != 24 else 28
     t0 = time.time()
-    g = gx.rmat_graph(scale, args.edge_factor, seed=SEED, P=256)
+    g = gx.rmat_graph(scale, args.edge_factor, seed=SEED, P=256, gpu=True)
     build_s = time.time() - t0
     budget = 8 << 30
     t1 = time.time()
@@ -440,7 +444,7 @@ def run_batch(args):
 
 def run_ppr(args):
     import graphee_gb300 as gx
-    g, build_s = build_graph(args)
+    g, build_s = build_graph(args, device=0)
     rng = np.random.default_rng(SEED)
     src = rng.integers(0, g.V, size=64).astype(np.int32)
     with gx.Engine() as e:
@@ -469,7 +473,7 @@ def run_warm(args):
         ja, jb, jc = rng.uniform(-0.05, 0.05, size=3)
         while 0.57 + ja + 0.19 + jb + 0.19 + jc > 0.99:   # keep d = 1 - a - b - c >= 0.01
             ja, jb, jc = rng.uniform(-0.05, 0.05, size=3)
-        g = gx.rmat_graph(s, 16, seed=SEED + 17 * i, P=16, a=0.57 + ja, b=0.19 + jb, c=0.19 + jc)
+        g = gx.rmat_graph(s, 16, seed=SEED + 17 * i, P=16, a=0.57 + ja, b=0.19 + jb, c=0.19 + jc, gpu=True)
         with gx.Engine() as e:
             e.load(g)
             m.add_graph(e, max_samples=65536, max_iter=500, tolerance=1e-9)
@@ -479,7 +483,7 @@ def run_warm(args):
     train_s = time.time() - t1
     evals = {}
     for scale in (24, 26):
-        g = gx.rmat_graph(scale, 16, seed=SEED + 99991 + scale, P=256)
+        g = gx.rmat_graph(scale, 16, seed=SEED + 99991 + scale, P=256, gpu=True)
         with gx.Engine() as e:
             e.load(g)
             e.run(gx.APP_PAGERANK_STD, 3)

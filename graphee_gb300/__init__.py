@@ -110,6 +110,8 @@ def lib() -> C.CDLL:
         "gx_create": (C.c_int, [P, P]),
         "gx_destroy": (C.c_int, [P]),
         "gx_release_cached_memory": (C.c_int, [I32]),
+        "gx_build_csc_gpu": (C.c_int, [I32, I32, I64, P, P, I32, P, P, P]),
+        "gx_rmat_csc_gpu": (C.c_int, [I32, I32, I64, D, D, D, U64, I32, P, P, P]),
         "gx_write_values_npy": (C.c_int, [P, C.c_char_p]),
         "gx_read_values_npy": (C.c_int, [C.c_char_p, I64, P]),
         "gx_load_shards": (C.c_int, [P, C.c_char_p, I32, I32]),
@@ -209,15 +211,46 @@ def build_csc(V: int, src, dst, flags=BUILD_DROP_SELF | BUILD_DEDUP):
     return off, col[:nout.value].copy()
 
 
+def build_csc_gpu(V: int, src, dst, flags=BUILD_DROP_SELF | BUILD_DEDUP, device: int = 0):
+    """build_csc computed on the GPU (same output)."""
+    src = np.ascontiguousarray(src, np.int32)
+    dst = np.ascontiguousarray(dst, np.int32)
+    n = len(src)
+    cap = 2 * n if flags & BUILD_SYMMETRIZE else n
+    off = np.empty(V + 1, np.int64)
+    col = np.empty(max(cap, 1), np.int32)
+    nout = C.c_int64(0)
+    _check(lib().gx_build_csc_gpu(device, V, n, _ptr(src), _ptr(dst), flags, _ptr(off), _ptr(col), C.byref(nout)),
+           "gx_build_csc_gpu")
+    return off, col[:nout.value].copy()
+
+
+def rmat_csc_gpu(scale: int, n: int, seed: int, a=0.57, b=0.19, c=0.19, flags=BUILD_DROP_SELF | BUILD_DEDUP,
+                 device: int = 0):
+    """The CSC of rmat_edges(scale, n, seed, a, b, c) built with `flags`,
+    generated and built on the GPU."""
+    cap = 2 * n if flags & BUILD_SYMMETRIZE else n
+    off = np.empty((1 << scale) + 1, np.int64)
+    col = np.empty(max(cap, 1), np.int32)
+    nout = C.c_int64(0)
+    _check(lib().gx_rmat_csc_gpu(device, scale, n, a, b, c, seed & 0xFFFFFFFFFFFFFFFF, flags, _ptr(off), _ptr(col),
+                                 C.byref(nout)), "gx_rmat_csc_gpu")
+    return off, col[:nout.value].copy()
+
+
 def rmat_graph(scale: int, edge_factor: int, seed: int, P: int = 1, symmetric=False, a=0.57, b=0.19, c=0.19,
-               weight_seed: int | None = None) -> Graph:
+               weight_seed: int | None = None, gpu: bool = False, device: int = 0) -> Graph:
     """Seeded R-MAT graph, self-loops and duplicates removed (optionally
-    symmetrised), as a Graph with P edge-balanced shards."""
+    symmetrised), as a Graph with P edge-balanced shards.  gpu=True
+    generates and builds it on GPU `device` (the same graph)."""
     V = 1 << scale
-    src, dst = rmat_edges(scale, edge_factor * V, seed, a, b, c)
     flags = BUILD_DROP_SELF | BUILD_DEDUP | (BUILD_SYMMETRIZE if symmetric else 0)
-    off, col = build_csc(V, src, dst, flags)
-    del src, dst
+    if gpu:
+        off, col = rmat_csc_gpu(scale, edge_factor * V, seed, a, b, c, flags, device)
+    else:
+        src, dst = rmat_edges(scale, edge_factor * V, seed, a, b, c)
+        off, col = build_csc(V, src, dst, flags)
+        del src, dst
     g = Graph(V, off, col, None, P)
     if weight_seed is not None:
         g.weights = edge_weights(weight_seed, g)

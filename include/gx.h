@@ -313,6 +313,19 @@ gx_status gx_rmat_edges(int32_t scale, int64_t n, double a, double b, double c,
 gx_status gx_build_csc(int32_t V, int64_t n, const int32_t* src, const int32_t* dst,
                        int32_t flags, int64_t* off, int32_t* col, int64_t* n_out);
 
+/* gx_build_csc computed on a GPU (`device`): same arguments, same output,
+ * bit for bit.  Keys (dst, src) are radix-sorted on the device and runs of
+ * equal keys collapse; replaces the offline Spark job and cal.cpp's degree
+ * pass (GraphMP/tools/format_spark.py, GraphMP/app/cal.cpp). */
+gx_status gx_build_csc_gpu(int32_t device, int32_t V, int64_t n, const int32_t* src, const int32_t* dst,
+                           int32_t flags, int64_t* off, int32_t* col, int64_t* n_out);
+
+/* The CSC of gx_rmat_edges(scale, n, a, b, c, seed, 0, ...) built by
+ * gx_build_csc(2^scale, ..., flags), with the edges generated and the CSC
+ * built on the GPU.  col must hold n entries (2n with GX_BUILD_SYMMETRIZE). */
+gx_status gx_rmat_csc_gpu(int32_t device, int32_t scale, int64_t n, double a, double b, double c, uint64_t seed,
+                          int32_t flags, int64_t* off, int32_t* col, int64_t* n_out);
+
 /* Edge-balanced destination-range shard boundaries, the rule of
  * GraphMP/tools/format_spark.py:91-108: bounds[i] = first v with
  * off[v] >= ceil(E/P)*i, bounds[0] = 0, bounds[P] = V. */
