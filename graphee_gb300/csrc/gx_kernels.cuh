@@ -260,6 +260,27 @@ constexpr int kLaneMaxDegree = GX_LANE_MAX;  // longest list a lane walks alone
 constexpr int kGrab = GX_GRAB;               // units a warp claims per atomic
 constexpr int kQueues = 64;          // work-unit cursors per launch
 
+// Queue q of nq splits U units evenly; its cursor counts units handed out.
+// Returns the first queue after q (cyclically) whose cursor is below its
+// size, reading every cursor in one round trip, or -1 when all are drained.
+__device__ __forceinline__ int next_queue(const unsigned int* ctr, int q, int nq, int64_t U, int lane) {
+  bool ok0 = false, ok1 = false;
+  if (lane < nq) {
+    const int64_t size = (U * (lane + 1)) / nq - (U * lane) / nq;
+    ok0 = static_cast<int64_t>(*reinterpret_cast<const volatile unsigned int*>(ctr + lane)) < size;
+  }
+  if (lane + 32 < nq) {
+    const int j = lane + 32;
+    const int64_t size = (U * (j + 1)) / nq - (U * j) / nq;
+    ok1 = static_cast<int64_t>(*reinterpret_cast<const volatile unsigned int*>(ctr + j)) < size;
+  }
+  const unsigned long long left = static_cast<unsigned long long>(__ballot_sync(0xffffffffu, ok0)) |
+                                  (static_cast<unsigned long long>(__ballot_sync(0xffffffffu, ok1)) << 32);
+  if (!left) return -1;
+  const unsigned long long after = q + 1 < 64 ? (left >> (q + 1)) << (q + 1) : 0ull;
+  return __ffsll(static_cast<long long>(after ? after : left)) - 1;
+}
+
 template <class T>
 __device__ __forceinline__ void store4(T* dst, const T (&x)[4]) {
   uint4 u;
@@ -372,21 +393,22 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
   LocalAcc la;
 
   // Units are split into up to kQueues contiguous ranges, each with its own
-  // cursor; a warp starts on queue (warp id mod queues) and moves on to the
-  // next queue when its own is drained, so cursors see little contention.
+  // cursor; a warp starts on queue (warp id mod queues).  When its queue is
+  // drained it reads every cursor at once (one round trip) and moves to the
+  // next queue with units left, or stops when none has any.
   const int U = a.u_end - a.u_begin;
   const int nq = U / 256 < 1 ? 1 : (U / 256 < kQueues ? U / 256 : kQueues);
   const int gw = blockIdx.x * kWarps + wid;
   int q = gw % nq;
-  for (int visited = 0; visited < nq;) {
+  for (;;) {
     const int qb = a.u_begin + static_cast<int>((static_cast<int64_t>(U) * q) / nq);
     const int qe = a.u_begin + static_cast<int>((static_cast<int64_t>(U) * (q + 1)) / nq);
     int u0 = 0;
     if (lane == 0) u0 = qb + static_cast<int>(atomicAdd(a.ctr + q, static_cast<unsigned>(kGrab)));
     u0 = __shfl_sync(0xffffffffu, u0, 0);
     if (u0 >= qe) {
-      q = q + 1 == nq ? 0 : q + 1;
-      ++visited;
+      q = next_queue(a.ctr, q, nq, U, lane);
+      if (q < 0) break;
       continue;
     }
     const int cnt = qe - u0 < kGrab ? qe - u0 : kGrab;

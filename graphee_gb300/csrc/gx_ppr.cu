@@ -59,15 +59,15 @@ __global__ void __launch_bounds__(kPprThreads) ppr_kernel(const PprArgs a) {
   const int U = a.n_units;
   const int nq = U / 256 < 1 ? 1 : (U / 256 < kQueues ? U / 256 : kQueues);
   int q = (blockIdx.x * kPprWarps + wid) % nq;
-  for (int visited = 0; visited < nq;) {
+  for (;;) {
     const int qb = static_cast<int>((static_cast<int64_t>(U) * q) / nq);
     const int qe = static_cast<int>((static_cast<int64_t>(U) * (q + 1)) / nq);
     int u0 = 0;
     if (lane == 0) u0 = qb + static_cast<int>(atomicAdd(a.ctr + q, 2u));
     u0 = __shfl_sync(0xffffffffu, u0, 0);
     if (u0 >= qe) {
-      q = q + 1 == nq ? 0 : q + 1;
-      ++visited;
+      q = next_queue(a.ctr, q, nq, U, lane);
+      if (q < 0) break;
       continue;
     }
     const int u1 = u0 + 2 < qe ? u0 + 2 : qe;
