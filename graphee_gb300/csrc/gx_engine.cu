@@ -780,9 +780,23 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
     }
     if (exec) cudaGraphExecDestroy(exec);
   } else {
-    // Host-driven steps: shard launches in order, streamed shards through
-    // the slot ring on the copy stream, overlapped with compute.
+    // Host-driven steps: one launch per shard, streamed shards through the
+    // slot ring on the copy stream, overlapped with compute.  A Jacobi step
+    // may sweep its shards in any order, so streamed shards are spread evenly
+    // among the resident ones: the copy engine then works through the whole
+    // step instead of waiting for the resident shards' compute.
     const int slots = static_cast<int>(e->slot_col.size());
+    std::vector<int32_t> order;
+    {
+      std::vector<int32_t> res, str;
+      for (int32_t p = 0; p < e->P; ++p) (e->resident[p] ? res : str).push_back(p);
+      const int64_t S = static_cast<int64_t>(str.size()), Pn = e->P;
+      size_t i_r = 0, i_s = 0;
+      for (int64_t pos = 0; pos < Pn; ++pos) {
+        const bool take_s = i_s < str.size() && (i_r >= res.size() || (2 * static_cast<int64_t>(i_s) + 1) * Pn <= 2 * pos * S);
+        order.push_back(take_s ? str[i_s++] : res[i_r++]);
+      }
+    }
     cudaEvent_t c0, c1, k0, k1;
     GX_CUDA(cudaEventCreate(&c0));
     GX_CUDA(cudaEventCreate(&c1));
@@ -798,7 +812,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
       const bool sel = hc.mode == MODE_SELECTIVE;
       GX_CUDA(cudaEventRecord(k0, e->s_comp));
       GX_CUDA(cudaEventRecord(c0, e->s_comp));
-      for (int32_t p = 0; p < e->P; ++p) {
+      for (const int32_t p : order) {
         PullArgs sp = pa;
         sp.u_begin = e->unit_begin[p];
         sp.u_end = e->unit_begin[p + 1];
