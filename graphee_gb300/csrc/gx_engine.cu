@@ -356,13 +356,129 @@ gx_status upload_async(gx_engine* e, void* dst, const void* src, size_t bytes, c
   return GX_OK;
 }
 
+gx_status setup_slot_events(gx_engine* e, int slots) {
+  if (static_cast<int>(e->slot_free.size()) >= slots) return GX_OK;
+  for (auto ev : e->slot_free) cudaEventDestroy(ev);
+  for (auto ev : e->slot_ready) cudaEventDestroy(ev);
+  e->slot_free.assign(slots, nullptr);
+  e->slot_ready.assign(slots, nullptr);
+  for (int i = 0; i < slots; ++i) {
+    GX_CUDA(cudaEventCreateWithFlags(&e->slot_free[i], cudaEventDisableTiming));
+    GX_CUDA(cudaEventCreateWithFlags(&e->slot_ready[i], cudaEventDisableTiming));
+  }
+  return GX_OK;
+}
+
+inline int64_t align16(int64_t x) { return (x + 15) & ~int64_t(15); }
+
+// The compressed streaming format.  Chunk c holds the source ids of global
+// edges [32c, 32c+32) as offsets from their minimum, nb bytes each, nb = 0..4
+// the fewest that hold the largest (comp_idx4 in gx_kernels.cuh reads them).
+// A streamed shard's blob: chunk headers (8 bytes each) | payload (32*nb bytes
+// per chunk, every chunk 16-byte aligned) | one byte per weight.  Chunks
+// straddling two shards are stored in both blobs.  Resident shards stay plain:
+// their compute is not slowed by decoding, and the copy engine, the bound of
+// a streamed superstep, moves fewer bytes.
+gx_status encode_streamed(gx_engine* e, const int32_t* col) {
+  const int32_t P = e->P;
+  const int64_t E = e->E;
+  const bool wt = e->has_weights;
+  e->cb_off.assign(P + 1, 0);
+  e->cb_bytes.assign(P, 0);
+  e->cb_c0.assign(P, 0);
+  e->cb_pay.assign(P, 0);
+  e->cb_w8.assign(P, 0);
+  std::vector<int64_t> nch(P, 0), c1s(P, 0);
+  for (int32_t p = 0; p < P; ++p) {
+    if (e->resident[p]) continue;
+    const int64_t e0 = e->off[e->bounds[p]], e1 = e->off[e->bounds[p + 1]];
+    e->cb_c0[p] = e0 >> 5;
+    c1s[p] = e1 > e0 ? (e1 + 31) >> 5 : e->cb_c0[p];
+    nch[p] = c1s[p] - e->cb_c0[p];
+  }
+  // Bytes per offset of every chunk of the streamed shards.
+  std::vector<std::vector<uint8_t>> width(P);
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int32_t p = 0; p < P; ++p) {
+    if (e->resident[p]) continue;
+    width[p].resize(static_cast<size_t>(nch[p]));
+    for (int64_t i = 0; i < nch[p]; ++i) {
+      const int64_t lo = 32 * (e->cb_c0[p] + i), hi = std::min(E, lo + 32);
+      uint32_t mn = static_cast<uint32_t>(col[lo]), mx = mn;
+      for (int64_t k = lo + 1; k < hi; ++k) {
+        const uint32_t x = static_cast<uint32_t>(col[k]);
+        mn = std::min(mn, x);
+        mx = std::max(mx, x);
+      }
+      uint32_t bits = 0;
+      for (uint32_t r = mx - mn; r; r >>= 1) ++bits;
+      width[p][i] = static_cast<uint8_t>((bits + 7) / 8);
+    }
+  }
+  // A shard travels compressed only when its blob is at most 85% of the
+  // plain bytes: otherwise the decoding costs more compute than the copy saves.
+  int64_t max_blob = 16, n_blobs = 0, n_streamed = 0;
+  for (int32_t p = 0; p < P; ++p) {
+    int64_t pay = 0;  // 32*nb bytes per chunk, a multiple of 16
+    for (int64_t i = 0; i < nch[p]; ++i) pay += 32 * width[p][i];
+    e->cb_pay[p] = align16(8 * nch[p]);
+    e->cb_w8[p] = align16(e->cb_pay[p] + pay);
+    const int64_t blob = align16(e->cb_w8[p] + (wt ? 32 * nch[p] : 0));
+    const int64_t plain = (e->off[e->bounds[p + 1]] - e->off[e->bounds[p]]) * (wt ? 8 : 4);
+    const bool use = !e->resident[p] && nch[p] > 0 && blob * 100 <= plain * 85;
+    n_streamed += !e->resident[p];
+    n_blobs += use;
+    e->cb_bytes[p] = use ? blob : 0;
+    e->cb_off[p + 1] = e->cb_off[p] + e->cb_bytes[p];
+    max_blob = std::max(max_blob, e->cb_bytes[p]);
+  }
+  e->comp_all = n_blobs == n_streamed;
+  if (e->h_cblob) cudaFreeHost(e->h_cblob);
+  e->h_cblob = nullptr;
+  GX_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->h_cblob), std::max<int64_t>(e->cb_off[P], 16),
+                        cudaHostAllocDefault));
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int32_t p = 0; p < P; ++p) {
+    if (e->cb_bytes[p] == 0) continue;
+    uint8_t* blob = e->h_cblob + e->cb_off[p];
+    uint2* hdr = reinterpret_cast<uint2*>(blob);
+    uint8_t* pay = blob + e->cb_pay[p];
+    uint8_t* w8 = blob + e->cb_w8[p];
+    memset(blob, 0, static_cast<size_t>(e->cb_bytes[p]));
+    uint32_t w16 = 0;  // payload position in 16-byte units
+    for (int64_t i = 0; i < nch[p]; ++i) {
+      const int64_t lo = 32 * (e->cb_c0[p] + i), hi = std::min(E, lo + 32);
+      const uint32_t nb = width[p][i];
+      uint32_t mn = static_cast<uint32_t>(col[lo]);
+      for (int64_t k = lo + 1; k < hi; ++k) mn = std::min(mn, static_cast<uint32_t>(col[k]));
+      hdr[i] = make_uint2(mn, (w16 << 3) | nb);
+      uint8_t* q = pay + static_cast<size_t>(w16) * 16;
+      for (int64_t k = lo; k < hi; ++k) {
+        const uint32_t v = static_cast<uint32_t>(col[k]) - mn;  // little-endian bytes
+        for (uint32_t t = 0; t < nb; ++t) q[(k - lo) * nb + t] = static_cast<uint8_t>(v >> (8 * t));
+      }
+      if (wt)
+        for (int64_t k = lo; k < hi; ++k) w8[i * 32 + (k - lo)] = static_cast<uint8_t>(e->h_w[k]);
+      w16 += 2 * nb;  // 32 * nb bytes
+    }
+  }
+  for (auto ptr : e->slot_blob) gx::pool_free(ptr);
+  e->slot_blob.assign(e->n_slots, nullptr);
+  for (int i = 0; i < e->n_slots; ++i) GX_TRY(dev_alloc(&e->slot_blob[i], static_cast<size_t>(max_blob)));
+  e->comp = n_blobs > 0;
+  e->comp_bytes = e->cb_off[P];
+  return GX_OK;
+}
+
 // Decides which shards stay in HBM under the budget (in shard order, like the
 // reference's insert-until-full edge cache, Global.h:170-244), uploads them,
-// and sets up the streaming ring for the rest.
+// and sets up the streaming ring for the rest.  When the plain shards exceed
+// the budget and compression is on, the compressed shard cache is used.
 gx_status plan_shards(gx_engine* e, const int32_t* src_col, bool col_on_device) {
   const int32_t P = e->P;
   const int64_t per_edge = e->has_weights ? 8 : 4;
   const int64_t budget = e->cfg.cache_budget_bytes;
+  e->comp = false;
   e->resident.assign(P, 0);
   e->dev_base.assign(P, 0);
   int64_t used = 0, max_stream = 0;
@@ -410,20 +526,32 @@ gx_status plan_shards(gx_engine* e, const int32_t* src_col, bool col_on_device) 
     }
     const int slots = std::max({2, e->cfg.stream_slots, static_cast<int>(e->s_copies.size())});
     e->slot_elems = max_stream + 8;
-    for (auto ptr : e->slot_col) cudaFree(ptr);
-    for (auto ptr : e->slot_w) cudaFree(ptr);
+    for (auto ptr : e->slot_col) gx::pool_free(ptr);
+    for (auto ptr : e->slot_w) gx::pool_free(ptr);
+    for (auto ptr : e->slot_blob) gx::pool_free(ptr);
+    e->slot_blob.clear();
     e->slot_col.assign(slots, nullptr);
     e->slot_w.assign(slots, nullptr);
     for (int i = 0; i < slots; ++i) {
       GX_TRY(dev_alloc(&e->slot_col[i], e->slot_elems));
       if (e->has_weights) GX_TRY(dev_alloc(&e->slot_w[i], e->slot_elems));
     }
-    if (e->slot_free.empty()) {
-      e->slot_free.resize(slots);
-      e->slot_ready.resize(slots);
-      for (int i = 0; i < slots; ++i) {
-        GX_CUDA(cudaEventCreateWithFlags(&e->slot_free[i], cudaEventDisableTiming));
-        GX_CUDA(cudaEventCreateWithFlags(&e->slot_ready[i], cudaEventDisableTiming));
+    e->n_slots = slots;
+    GX_TRY(setup_slot_events(e, slots));
+    // Streamed shards travel compressed when the weights (if any) fit bytes.
+    if (e->cfg.compress_cache && (!e->has_weights || e->w_narrow)) {
+      // A chunk header addresses the payload in 16-byte units with 29 bits,
+      // far beyond any shard of fewer than 2^31 edges.
+      GX_TRY(encode_streamed(e, src_col));
+      // With every streamed shard compressed, the plain ring is only needed
+      // for the shard signatures.
+      if (e->comp && e->comp_all) {
+        for (int i = 1; i < slots; ++i) {
+          gx::pool_free(e->slot_col[i]);
+          if (!e->slot_w.empty() && e->slot_w[i]) gx::pool_free(e->slot_w[i]);
+        }
+        e->slot_col.resize(1);
+        if (!e->slot_w.empty()) e->slot_w.resize(1);
       }
     }
   }
@@ -448,7 +576,7 @@ gx_status build_signatures(gx_engine* e) {
     signature_all_kernel<<<e->n_sm * 8, 256, 0, e->s_comp>>>(e->d_sig, e->d_col, d_eb, P, e->shard_group, e->V);
     cudaError_t err = cudaGetLastError();
     if (err == cudaSuccess) err = cudaStreamSynchronize(e->s_comp);
-    cudaFree(d_eb);
+    gx::pool_free(d_eb);
     if (err != cudaSuccess) return fail(GX_ERR_CUDA, "signatures: %s", cudaGetErrorString(err));
     return GX_OK;
   }
@@ -500,7 +628,7 @@ gx_status build_out_edges(gx_engine* e, bool weighted) {
                                                         e->d_ocol, weighted ? e->d_ow : nullptr);
   cudaError_t err = cudaGetLastError();
   if (err == cudaSuccess) err = cudaStreamSynchronize(e->s_comp);
-  cudaFree(cursor);
+  gx::pool_free(cursor);
   if (err != cudaSuccess) return fail(GX_ERR_CUDA, "transpose: %s", cudaGetErrorString(err));
   e->out_built = true;
   e->out_weighted = weighted;
@@ -785,7 +913,13 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
     // may sweep its shards in any order, so streamed shards are spread evenly
     // among the resident ones: the copy engine then works through the whole
     // step instead of waiting for the resident shards' compute.
-    const int slots = static_cast<int>(e->slot_col.size());
+    const int slots = e->n_slots;
+    // Compressed shards are read by the COMP variant of the pull kernel.
+    void (*pull_comp)(PullArgs) = e->cfg.exact_order ? pull_kernel<APP, true, false, true>
+                                                     : pull_kernel<APP, false, false, true>;
+    if constexpr (APP == K_SSSP_UNIT || APP == K_SSSP_W || APP == K_CC) {
+      if (c.async_mode) pull_comp = pull_kernel<APP, false, true, true>;
+    }
     std::vector<int32_t> order;
     {
       std::vector<int32_t> res, str;
@@ -819,7 +953,23 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
         sp.ctr = e->d_work + 2 * kQueues + kQueues * p;
         if (sp.u_end == sp.u_begin) continue;
         const bool active = !sel || ((hc.shard_mask >> (p / e->shard_group)) & 1ull);
-        if (e->resident[p] || !active) {
+        const bool use_comp = e->comp && !e->resident[p] && active && e->cb_bytes[p] > 0;
+        if (use_comp) {
+          cudaStream_t cs = e->s_copies[slot % e->s_copies.size()];
+          GX_CUDA(cudaStreamWaitEvent(cs, e->slot_free[slot], 0));
+          GX_CUDA(cudaMemcpyAsync(e->slot_blob[slot], e->h_cblob + e->cb_off[p], e->cb_bytes[p],
+                                  cudaMemcpyHostToDevice, cs));
+          h2d_bytes += e->cb_bytes[p];
+          GX_CUDA(cudaEventRecord(e->slot_ready[slot], cs));
+          GX_CUDA(cudaStreamWaitEvent(e->s_comp, e->slot_ready[slot], 0));
+          const uint8_t* base = e->slot_blob[slot];
+          sp.col = nullptr;
+          sp.w = nullptr;
+          sp.chdr = reinterpret_cast<const uint2*>(base) - e->cb_c0[p];
+          sp.cpay = reinterpret_cast<const uint32_t*>(base + e->cb_pay[p]);
+          sp.w8 = base + e->cb_w8[p] - 32 * e->cb_c0[p];
+          ++streamed;
+        } else if (e->resident[p] || !active) {
           sp.col = e->d_col + e->dev_base[p];
           if (e->d_w) sp.w = e->d_w + e->dev_base[p];
         } else {
@@ -843,7 +993,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
         }
         const int units = sp.u_end - sp.u_begin;
         const int grid = std::max(1, std::min(grid_pull, (units + kWarps - 1) / kWarps));
-        pull<<<grid, kThreads, 0, e->s_comp>>>(sp);
+        if (use_comp) pull_comp<<<grid, kThreads, 0, e->s_comp>>>(sp);
+        else pull<<<grid, kThreads, 0, e->s_comp>>>(sp);
         GX_CUDA(cudaGetLastError());
         ++launches;
         ++pull_launches;
@@ -939,6 +1090,7 @@ void gx_config_default(gx_config* cfg) {
   cfg->profile = 0;
   cfg->layout = 0;
   cfg->push_edge_fraction = 0.5;
+  cfg->compress_cache = 1;
 }
 
 void gx_run_params_default(gx_run_params* p, gx_app app) {
@@ -1184,7 +1336,7 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
     unsigned int h = 0;
     cudaError_t err = cudaMemcpyAsync(&h, flag, sizeof(h), cudaMemcpyDeviceToHost, e->s_comp);
     if (err == cudaSuccess) err = cudaStreamSynchronize(e->s_comp);
-    cudaFree(flag);
+    gx::pool_free(flag);
     if (err != cudaSuccess) return fail(GX_ERR_CUDA, "gx_load_csc validation: %s", cudaGetErrorString(err));
     if (h & 1u) {
       e->release_graph();
@@ -1245,6 +1397,13 @@ gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
   memcpy(e->h_w, w, e->E * sizeof(uint32_t));
   memset(e->h_w + e->E, 0, 8 * sizeof(uint32_t));
   e->has_weights = true;
+  {
+    uint32_t mx = 0;
+    const int64_t E = e->E;
+#pragma omp parallel for reduction(max : mx)
+    for (int64_t k = 0; k < E; ++k) mx = std::max(mx, w[k]);
+    e->w_narrow = mx <= 255u;  // byte weights in the compressed shard cache
+  }
   if (e->all_resident) {
     // Resident plan with the weights: re-plan against the budget, which now
     // counts 8 bytes per edge.

@@ -33,7 +33,7 @@ namespace gx {
 // after another engine was destroyed maps no new memory and destroying an
 // engine unmaps none.  gx_release_cached_memory() trims the pool.  Blocks are
 // handed out and returned on a private stream that is synchronised after each
-// call; callers free only memory no running kernel uses.
+// call.
 struct DevicePool {
   cudaMemPool_t pool = nullptr;
   cudaStream_t stream = nullptr;
@@ -49,6 +49,9 @@ inline cudaError_t pool_malloc(void** p, size_t bytes) {
   return err;
 }
 
+// Frees a block of the pool once no work on the device can still use it
+// (a pool block is never freed with cudaFree, which neither waits for that
+// work nor goes through the pool's bookkeeping).
 inline void pool_free(void* p) {
   if (!p) return;
   DevicePool* dp = device_pool(current_device());
@@ -56,6 +59,7 @@ inline void pool_free(void* p) {
     cudaFree(p);
     return;
   }
+  cudaDeviceSynchronize();
   cudaFreeAsync(p, dp->stream);
   cudaStreamSynchronize(dp->stream);
 }
@@ -151,6 +155,18 @@ struct gx_engine {
   std::vector<int32_t*> slot_col;
   std::vector<uint32_t*> slot_w;
   std::vector<cudaEvent_t> slot_free, slot_ready;
+  int32_t n_slots = 0;
+
+  // Compressed streaming (compress_cache on): each streamed shard is a blob
+  // of chunk headers, byte offsets and byte weights (gx_kernels.cuh:
+  // comp_idx4) in the pinned h_cblob, copied through slot_blob.
+  bool comp = false;                // some streamed shard travels compressed
+  bool comp_all = false;            // every streamed shard does
+  bool w_narrow = false;            // every weight fits a byte
+  uint8_t* h_cblob = nullptr;
+  std::vector<int64_t> cb_off, cb_bytes, cb_c0, cb_pay, cb_w8;  // per shard
+  std::vector<uint8_t*> slot_blob;
+  int64_t comp_bytes = 0;           // all streamed blobs
 
   // device
   int64_t* d_off = nullptr;
@@ -248,10 +264,15 @@ struct gx_engine {
     gx::dev_free(&d_bpartial);
     gx::dev_free(&d_bticket);
     blocks_ready = false;
-    for (auto p : slot_col) cudaFree(p);
-    for (auto p : slot_w) cudaFree(p);
+    for (auto p : slot_col) gx::pool_free(p);
+    for (auto p : slot_w) gx::pool_free(p);
+    for (auto p : slot_blob) gx::pool_free(p);
     slot_col.clear();
     slot_w.clear();
+    slot_blob.clear();
+    if (h_cblob) cudaFreeHost(h_cblob);
+    h_cblob = nullptr;
+    comp = false;
     for (auto ev : slot_free) cudaEventDestroy(ev);
     for (auto ev : slot_ready) cudaEventDestroy(ev);
     slot_free.clear();

@@ -85,6 +85,11 @@ struct PullArgs {
   unsigned int* ctr;        // kQueues work-unit cursors of this launch (reset by finalize)
   int32_t heavy_deg;        // lists longer than this are swept by their own units
   uint32_t* bm;             // next-frontier bitmap
+  // Compressed shard (COMP launches): chunk headers indexed by global chunk
+  // id (edge >> 5), payload words, and byte weights indexed by global edge id.
+  const uint2* chdr;
+  const uint32_t* cpay;
+  const uint8_t* w8;
 };
 
 struct PushArgs {
@@ -324,10 +329,61 @@ __device__ __forceinline__ void flush_block(Ctl* ctl, const LocalAcc& la) {
   }
 }
 
+// Compressed shard format: the source ids of global edges [32c, 32c+32) form
+// chunk c, stored as hdr[c] = (min, w16 << 3 | nb) and 32 offsets id - min of
+// nb bytes each (nb = 0..4, the fewest that hold the largest), at byte
+// 16 * w16 of the payload.  Returns the ids of edges k..k+3 (k a multiple of
+// 4: all four lie in one chunk, and their bytes start 4-byte aligned, 8-byte
+// for nb = 2, 16-byte for nb = 4).
+__device__ __forceinline__ int4 comp_idx4(const uint2* hdr, const uint32_t* pay, int64_t k) {
+  const uint2 h = __ldg(hdr + (k >> 5));
+  const uint32_t nb = h.y & 7u;
+  const uint32_t j0 = static_cast<uint32_t>(k & 31);
+  const unsigned char* p = reinterpret_cast<const unsigned char*>(pay) + static_cast<size_t>(h.y >> 3) * 16 + j0 * nb;
+  uint32_t v0 = 0, v1 = 0, v2 = 0, v3 = 0;
+  if (nb == 1) {
+    const uint32_t x = __ldg(reinterpret_cast<const unsigned int*>(p));
+    v0 = x & 255u, v1 = (x >> 8) & 255u, v2 = (x >> 16) & 255u, v3 = x >> 24;
+  } else if (nb == 2) {
+    const uint2 x = __ldg(reinterpret_cast<const uint2*>(p));
+    v0 = x.x & 0xffffu, v1 = x.x >> 16, v2 = x.y & 0xffffu, v3 = x.y >> 16;
+  } else if (nb == 3) {
+    const unsigned int* q = reinterpret_cast<const unsigned int*>(p);
+    const uint32_t w0 = __ldg(q), w1 = __ldg(q + 1), w2 = __ldg(q + 2);
+    v0 = w0 & 0xffffffu;
+    v1 = (w0 >> 24) | ((w1 & 0xffffu) << 8);
+    v2 = (w1 >> 16) | ((w2 & 0xffu) << 16);
+    v3 = w2 >> 8;
+  } else if (nb == 4) {
+    const uint4 x = __ldg(reinterpret_cast<const uint4*>(p));
+    v0 = x.x, v1 = x.y, v2 = x.z, v3 = x.w;
+  }
+  const uint32_t m = h.x;
+  return make_int4(static_cast<int>(m + v0), static_cast<int>(m + v1), static_cast<int>(m + v2),
+                   static_cast<int>(m + v3));
+}
+
+// Source ids / weights of edges k..k+3 (k a multiple of 4): 128-bit loads of
+// the plain arrays, or the compressed shard's chunk and byte weights.
+template <bool COMP>
+__device__ __forceinline__ int4 load_idx4(const PullArgs& a, int64_t k) {
+  if constexpr (COMP) return comp_idx4(a.chdr, a.cpay, k);
+  else return __ldcs(reinterpret_cast<const int4*>(a.col + k));
+}
+template <bool COMP>
+__device__ __forceinline__ uint4 load_w4(const PullArgs& a, int64_t k) {
+  if constexpr (COMP) {
+    const uint32_t x = __ldcs(reinterpret_cast<const unsigned int*>(a.w8 + k));
+    return make_uint4(x & 255u, (x >> 8) & 255u, (x >> 16) & 255u, x >> 24);
+  } else {
+    return __ldcs(reinterpret_cast<const uint4*>(a.w + k));
+  }
+}
+
 // Warp-cooperative reduction of the edge range [b, e) (all lanes call it with
 // the same range): lanes take 8 consecutive edges each per round, with
 // 128-bit loads; the per-lane partials are combined by a fixed xor tree.
-template <int APP, bool ASYNC = false>
+template <int APP, bool ASYNC = false, bool COMP = false>
 __device__ __forceinline__ typename AppTraits<APP>::T warp_reduce_range(const PullArgs& a, const void* src_val,
                                                                         const float* src_con, int64_t b, int64_t e,
                                                                         int lane) {
@@ -335,13 +391,13 @@ __device__ __forceinline__ typename AppTraits<APP>::T warp_reduce_range(const Pu
   T acc = identity<APP>();
   for (int64_t q = (b & ~3ll) + 4 * lane; q < e; q += 256) {
     const int64_t q2 = q + 128;
-    const int4 c4 = __ldcs(reinterpret_cast<const int4*>(a.col + q));
+    const int4 c4 = load_idx4<COMP>(a, q);
     int4 d4 = make_int4(0, 0, 0, 0);
-    if (q2 < e) d4 = __ldcs(reinterpret_cast<const int4*>(a.col + q2));
+    if (q2 < e) d4 = load_idx4<COMP>(a, q2);
     uint4 w4 = make_uint4(0, 0, 0, 0), x4 = make_uint4(0, 0, 0, 0);
     if constexpr (APP == K_SSSP_W) {
-      w4 = __ldcs(reinterpret_cast<const uint4*>(a.w + q));
-      if (q2 < e) x4 = __ldcs(reinterpret_cast<const uint4*>(a.w + q2));
+      w4 = load_w4<COMP>(a, q);
+      if (q2 < e) x4 = load_w4<COMP>(a, q2);
     }
     const int cs[8] = {c4.x, c4.y, c4.z, c4.w, d4.x, d4.y, d4.z, d4.w};
     const uint32_t ws[8] = {w4.x, w4.y, w4.z, w4.w, x4.x, x4.y, x4.z, x4.w};
@@ -363,7 +419,7 @@ __device__ __forceinline__ typename AppTraits<APP>::T warp_reduce_range(const Pu
 #define GX_PULL_MIN_BLOCKS 4
 #endif
 
-template <int APP, bool EXACT, bool ASYNC = false>
+template <int APP, bool EXACT, bool ASYNC = false, bool COMP = false>
 __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(PullArgs a) {
   typedef typename AppTraits<APP>::T T;
   __shared__ __align__(16) T s_buf[EXACT ? kWarps : 1][EXACT ? kChunk : 4];
@@ -458,7 +514,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
         const int64_t b = vb + static_cast<int64_t>(wu.y) * kHeavyChunk;
         const int64_t e = ve < b + kHeavyChunk ? ve : b + kHeavyChunk;
         T acc = identity<APP>();
-        if constexpr (APP != K_INDEG) acc = warp_reduce_range<APP, ASYNC>(a, src_val, src_con, b, e, lane);
+        if constexpr (APP != K_INDEG) acc = warp_reduce_range<APP, ASYNC, COMP>(a, src_val, src_con, b, e, lane);
         if (lane == 0) {
           la.edges += e - b;
           T* part = static_cast<T*>(a.partial);
@@ -533,9 +589,9 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
             for (int j = 0; j < kChunk / 128; ++j) {
               const int64_t q = c0 + 4 * (lane + 32 * j);
               if (q < E1) {
-                const int4 c4 = __ldcs(reinterpret_cast<const int4*>(a.col + q));
+                const int4 c4 = load_idx4<COMP>(a, q);
                 uint4 w4 = make_uint4(0, 0, 0, 0);
-                if constexpr (APP == K_SSSP_W) w4 = __ldcs(reinterpret_cast<const uint4*>(a.w + q));
+                if constexpr (APP == K_SSSP_W) w4 = load_w4<COMP>(a, q);
                 const int cs[4] = {c4.x, c4.y, c4.z, c4.w};
                 const uint32_t ws[4] = {w4.x, w4.y, w4.z, w4.w};
                 T x[4];
@@ -548,10 +604,14 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
               }
             }
             __syncwarp();
-            const int lo = static_cast<int>((beg > c0 ? beg : c0) - c0);
-            const int hi = static_cast<int>((end < c0 + kChunk ? end : c0 + kChunk) - c0);
+            // Only a lane whose list meets the window folds: lo and hi then lie
+            // in [0, kChunk] (a difference of 64-bit edge ids never reaches int).
+            if (beg < c0 + kChunk && end > c0) {
+              const int lo = static_cast<int>((beg > c0 ? beg : c0) - c0);
+              const int hi = static_cast<int>((end < c0 + kChunk ? end : c0 + kChunk) - c0);
 #pragma unroll 4
-            for (int kk = lo; kk < hi; ++kk) acc = combine<APP>(acc, buf[kk]);
+              for (int kk = lo; kk < hi; ++kk) acc = combine<APP>(acc, buf[kk]);
+            }
             __syncwarp();
           }
         } else {
@@ -563,11 +623,11 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
           int4 c0v = make_int4(0, 0, 0, 0), c1v = make_int4(0, 0, 0, 0);
           uint4 w0v = make_uint4(0, 0, 0, 0), w1v = make_uint4(0, 0, 0, 0);
           if (steps > 0) {
-            c0v = __ldcs(reinterpret_cast<const int4*>(a.col + k));
-            if (k + 4 < lend) c1v = __ldcs(reinterpret_cast<const int4*>(a.col + k + 4));
+            c0v = load_idx4<COMP>(a, k);
+            if (k + 4 < lend) c1v = load_idx4<COMP>(a, k + 4);
             if constexpr (APP == K_SSSP_W) {
-              w0v = __ldcs(reinterpret_cast<const uint4*>(a.w + k));
-              if (k + 4 < lend) w1v = __ldcs(reinterpret_cast<const uint4*>(a.w + k + 4));
+              w0v = load_w4<COMP>(a, k);
+              if (k + 4 < lend) w1v = load_w4<COMP>(a, k + 4);
             }
           }
           for (int st = 0; st < smax; ++st) {
@@ -576,11 +636,11 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
               const uint32_t ws[8] = {w0v.x, w0v.y, w0v.z, w0v.w, w1v.x, w1v.y, w1v.z, w1v.w};
               const int64_t kn = k + 8;
               if (kn < lend) {
-                c0v = __ldcs(reinterpret_cast<const int4*>(a.col + kn));
-                if (kn + 4 < lend) c1v = __ldcs(reinterpret_cast<const int4*>(a.col + kn + 4));
+                c0v = load_idx4<COMP>(a, kn);
+                if (kn + 4 < lend) c1v = load_idx4<COMP>(a, kn + 4);
                 if constexpr (APP == K_SSSP_W) {
-                  w0v = __ldcs(reinterpret_cast<const uint4*>(a.w + kn));
-                  if (kn + 4 < lend) w1v = __ldcs(reinterpret_cast<const uint4*>(a.w + kn + 4));
+                  w0v = load_w4<COMP>(a, kn);
+                  if (kn + 4 < lend) w1v = load_w4<COMP>(a, kn + 4);
                 }
               }
               T vals[8];
@@ -603,7 +663,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
             const int l = __ffs(m) - 1;
             const int64_t bl = __shfl_sync(0xffffffffu, beg, l);
             const int64_t el = __shfl_sync(0xffffffffu, end, l);
-            const T r = warp_reduce_range<APP, ASYNC>(a, src_val, src_con, bl, el, lane);
+            const T r = warp_reduce_range<APP, ASYNC, COMP>(a, src_val, src_con, bl, el, lane);
             if (lane == l) acc = combine<APP>(acc, r);
           }
         }

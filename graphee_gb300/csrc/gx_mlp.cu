@@ -643,7 +643,7 @@ gx_status compute_norm(gx_mlp* m) {
   std::vector<double> h(static_cast<size_t>(grid) * 2 * kF);
   cudaError_t err = cudaMemcpyAsync(h.data(), part, h.size() * sizeof(double), cudaMemcpyDeviceToHost, m->s);
   if (err == cudaSuccess) err = cudaStreamSynchronize(m->s);
-  cudaFree(part);
+  gx::pool_free(part);
   if (err != cudaSuccess) return fail(GX_ERR_CUDA, "mlp norm: %s", cudaGetErrorString(err));
   float nrm[2 * kF];
   for (int f = 0; f < kF; ++f) {
@@ -805,7 +805,7 @@ gx_status gx_mlp_add_graph(gx_mlp* m, gx_engine* e, int32_t max_samples, int32_t
   const float* rank = static_cast<const float*>(e->d_val[e->h_ctl->cur & 1]);
   float* feat = nullptr;
   GX_TRY(dev_alloc(&feat, static_cast<size_t>(V) * kFeatStride));
-  std::unique_ptr<float, void (*)(float*)> fg(feat, [](float* q) { cudaFree(q); });
+  std::unique_ptr<float, void (*)(float*)> fg(feat, [](float* q) { gx::pool_free(q); });
   FeatScratch fs;
   GX_TRY(fs.alloc(e));
   GX_TRY(engine_features(e, p.damping, feat, nullptr, m->s, fs));
@@ -884,9 +884,9 @@ gx_status gx_mlp_grad(gx_mlp* m, const float* host_x, const float* host_t, int32
   GX_CUDA(cudaSetDevice(m->dev));
   float *x = nullptr, *t = nullptr;
   GX_TRY(dev_alloc(&x, static_cast<size_t>(n) * kFeatStride));
-  std::unique_ptr<float, void (*)(float*)> gx_(x, [](float* q) { cudaFree(q); });
+  std::unique_ptr<float, void (*)(float*)> gx_(x, [](float* q) { gx::pool_free(q); });
   GX_TRY(dev_alloc(&t, static_cast<size_t>(n)));
-  std::unique_ptr<float, void (*)(float*)> gt_(t, [](float* q) { cudaFree(q); });
+  std::unique_ptr<float, void (*)(float*)> gt_(t, [](float* q) { gx::pool_free(q); });
   std::vector<float> hx(static_cast<size_t>(n) * kFeatStride, 0.f);
   for (int32_t i = 0; i < n; ++i)
     for (int f = 0; f < kF; ++f) hx[static_cast<size_t>(i) * kFeatStride + f] = host_x[static_cast<size_t>(i) * kF + f];
@@ -918,17 +918,17 @@ gx_status gx_mlp_predict(gx_mlp* m, gx_engine* e, double damping, float* host_ou
   cudaStream_t s = e->s_comp;
   float *feat = nullptr, *sv = nullptr;
   GX_TRY(dev_alloc(&feat, static_cast<size_t>(V) * kFeatStride));
-  std::unique_ptr<float, void (*)(float*)> fg(feat, [](float* q) { cudaFree(q); });
+  std::unique_ptr<float, void (*)(float*)> fg(feat, [](float* q) { gx::pool_free(q); });
   GX_TRY(dev_alloc(&sv, static_cast<size_t>(V)));
-  std::unique_ptr<float, void (*)(float*)> sg(sv, [](float* q) { cudaFree(q); });
+  std::unique_ptr<float, void (*)(float*)> sg(sv, [](float* q) { gx::pool_free(q); });
   FeatScratch fs;
   GX_TRY(fs.alloc(e));
   const int grid = e->n_sm * 8;
   double *ps = nullptr, *pd = nullptr;
   GX_TRY(dev_alloc(&ps, static_cast<size_t>(grid)));
-  std::unique_ptr<double, void (*)(double*)> psg(ps, [](double* q) { cudaFree(q); });
+  std::unique_ptr<double, void (*)(double*)> psg(ps, [](double* q) { gx::pool_free(q); });
   GX_TRY(dev_alloc(&pd, static_cast<size_t>(grid)));
-  std::unique_ptr<double, void (*)(double*)> pdg(pd, [](double* q) { cudaFree(q); });
+  std::unique_ptr<double, void (*)(double*)> pdg(pd, [](double* q) { gx::pool_free(q); });
   cudaEvent_t ev[3];
   for (auto& x : ev) GX_CUDA(cudaEventCreate(&x));
   GX_CUDA(cudaEventRecord(ev[0], s));

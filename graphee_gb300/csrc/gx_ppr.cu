@@ -168,7 +168,7 @@ extern "C" gx_status gx_ppr(gx_engine* e, int32_t k, const int32_t* sources, int
   struct Guard {
     std::vector<void*> p;
     ~Guard() {
-      for (void* x : p) cudaFree(x);
+      for (void* x : p) gx::pool_free(x);
     }
   } guard;
   gx_status st = GX_OK;

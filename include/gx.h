@@ -78,6 +78,11 @@ typedef struct gx_config {
   int32_t profile;             /* time every pull launch with CUDA events (default 0) */
   int32_t layout;              /* resident pull layout: 0 = warp work units (default), 1 = TMA-staged
                                   blocks (edges re-laid per shard, cp.async.bulk double buffering) */
+  int32_t compress_cache;      /* with a budget the plain shards exceed: keep every shard compressed
+                                  (source ids as per-32-edge byte offsets from their minimum, weights as
+                                  bytes when all fit), in HBM while the budget lasts and streamed
+                                  otherwise; decoded in the pull kernel, same results as plain
+                                  shards (default 1) */
   double push_edge_fraction;   /* SSSP/CC with push_sparse: also push when the frontier's out-edges are
                                   at most this fraction of E (default 0.5; 0 = push only when the
                                   step is selective, as the reference schedules it) */
