@@ -50,16 +50,37 @@ struct BatchArgs {
 };
 
 // Gathers a vertex's in-edge values: PR contributions (sum) or labels (min).
+// Lanes walk lists of up to lane_max edges alone, 8 edges per step from two
+// 128-bit index loads (edge order kept: positions outside the list are
+// masked), so each lane has 8 gathers in flight; longer lists are swept by the
+// whole warp, 4 consecutive edges per lane per round.
 template <bool PR>
 __device__ __forceinline__ void batch_vertex_lists(const BatchArgs& a, const float* con, const int32_t* lab,
                                                    int64_t beg, int64_t end, bool valid, float& facc, int32_t& iacc,
                                                    int lane) {
   const bool longl = valid && end - beg > a.lane_max;
-  if (valid && !longl) {
-    for (int64_t k = beg; k < end; ++k) {
-      const int32_t u = __ldg(a.col + k);
-      if (PR) facc += __ldg(con + u);
-      else iacc = min(iacc, __ldg(lab + u));
+  if (valid && !longl && end > beg) {
+    for (int64_t k = beg & ~3ll; k < end; k += 8) {
+      const int4 c0 = __ldg(reinterpret_cast<const int4*>(a.col + k));
+      int4 c1 = make_int4(0, 0, 0, 0);
+      if (k + 4 < end) c1 = __ldg(reinterpret_cast<const int4*>(a.col + k + 4));
+      const int32_t cs[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+      float fv[8];
+      int32_t iv[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const bool in = k + j >= beg && k + j < end;
+        if (PR) fv[j] = in ? __ldg(con + cs[j]) : 0.f;
+        else iv[j] = in ? __ldg(lab + cs[j]) : 0x7fffffff;
+      }
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if (PR) {
+          if (k + j >= beg && k + j < end) facc += fv[j];
+        } else {
+          iacc = min(iacc, iv[j]);
+        }
+      }
     }
   }
   for (unsigned m = __ballot_sync(0xffffffffu, longl); m; m &= m - 1) {
@@ -67,10 +88,16 @@ __device__ __forceinline__ void batch_vertex_lists(const BatchArgs& a, const flo
     const int64_t bl = __shfl_sync(0xffffffffu, beg, l), el = __shfl_sync(0xffffffffu, end, l);
     float fs = 0.f;
     int32_t is = 0x7fffffff;
-    for (int64_t k = bl + lane; k < el; k += 32) {
-      const int32_t u = __ldg(a.col + k);
-      if (PR) fs += __ldg(con + u);
-      else is = min(is, __ldg(lab + u));
+    for (int64_t q = (bl & ~3ll) + 4 * lane; q < el; q += 128) {
+      const int4 c = __ldg(reinterpret_cast<const int4*>(a.col + q));
+      const int32_t cs[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (q + j >= bl && q + j < el) {
+          if (PR) fs += __ldg(con + cs[j]);
+          else is = min(is, __ldg(lab + cs[j]));
+        }
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {

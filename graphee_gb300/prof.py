@@ -10,14 +10,48 @@ import argparse
 import json
 import time
 
+import numpy as np
+
 import graphee_gb300 as gx
 
 APPS = {"pagerank": gx.APP_PAGERANK_REF, "pagerank_std": gx.APP_PAGERANK_STD, "sssp": gx.APP_SSSP, "cc": gx.APP_CC}
+OTHER = ["tc", "ppr", "batch", "warm", "build"]
+
+
+def run_other(a):
+    """Workloads beside the superstep loop, one each, for a profiler."""
+    t0 = time.perf_counter()
+    if a.app == "build":
+        g = gx.rmat_graph(a.scale, a.edge_factor, seed=20240601, gpu=True)
+        print(json.dumps({"V": g.V, "E": g.E, "wall_s": time.perf_counter() - t0}))
+        return
+    if a.app == "batch":
+        g, vb = gx.batch_graph(256, scales=(10, 15), edge_factors=(8, 32), seed=20240601)
+        with gx.Engine() as e:
+            e.load(g)
+            out = e.batch_run(vb, 30, 1000)
+        print(json.dumps({"V": g.V, "E": g.E, "stats": out[-1]}, default=str))
+        return
+    sym = a.app == "tc"
+    g = gx.rmat_graph(a.scale, a.edge_factor, seed=20240601, P=256, symmetric=sym, gpu=True)
+    with gx.Engine() as e:
+        e.load(g)
+        if a.app == "tc":
+            n, st = e.triangle_count()
+            st["triangles"] = n
+        elif a.app == "ppr":
+            src = np.random.default_rng(1).integers(0, g.V, size=64).astype(np.int32)
+            st = e.ppr(src, a.iters, fetch=False)[1]
+        else:
+            m = gx.MLP(seed=1)
+            st = e.pagerank_warm(m, max_iter=a.iters)
+        st.update({"V": g.V, "E": g.E, "wall_s": time.perf_counter() - t0})
+        print(json.dumps(st))
 
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--app", default="pagerank", choices=sorted(APPS))
+    ap.add_argument("--app", default="pagerank", choices=sorted(APPS) + OTHER)
     ap.add_argument("--scale", type=int, default=22)
     ap.add_argument("--edge-factor", type=int, default=16)
     ap.add_argument("--iters", type=int, default=3)
@@ -27,6 +61,9 @@ def main():
     ap.add_argument("--tile-edges", type=int, default=None)
     ap.add_argument("--profile-kernels", type=int, default=0, help="time each pull launch with CUDA events")
     a = ap.parse_args()
+    if a.app in OTHER:
+        run_other(a)
+        return
     sym = a.app == "cc"
     g = gx.rmat_graph(a.scale, a.edge_factor, seed=20240601, P=256, symmetric=sym,
                       weight_seed=7 if a.app == "sssp" else None)
