@@ -19,6 +19,7 @@
 #include <omp.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -563,6 +564,7 @@ gx_status plan_shards(gx_engine* e, const int32_t* src_col, bool col_on_device) 
 // through slot 0).
 gx_status build_signatures(gx_engine* e) {
   const int32_t P = e->P;
+  e->sig_ready = false;
   e->shard_group = (P + 63) / 64;
   GX_TRY(dev_alloc(&e->d_sig, static_cast<size_t>(e->V)));
   GX_CUDA(cudaMemsetAsync(e->d_sig, 0, sizeof(unsigned long long) * e->V, e->s_comp));
@@ -578,6 +580,7 @@ gx_status build_signatures(gx_engine* e) {
     if (err == cudaSuccess) err = cudaStreamSynchronize(e->s_comp);
     gx::pool_free(d_eb);
     if (err != cudaSuccess) return fail(GX_ERR_CUDA, "signatures: %s", cudaGetErrorString(err));
+    e->sig_ready = true;
     return GX_OK;
   }
   for (int32_t p = 0; p < P; ++p) {
@@ -601,6 +604,7 @@ gx_status build_signatures(gx_engine* e) {
     GX_CUDA(cudaGetLastError());
   }
   GX_CUDA(cudaStreamSynchronize(e->s_comp));
+  e->sig_ready = true;
   return GX_OK;
 }
 
@@ -668,6 +672,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   c.push_ok = push_ok;
   c.push_edge_limit =
       push_ok ? static_cast<unsigned long long>(e->cfg.push_edge_fraction * static_cast<double>(e->E)) : 0ull;
+  c.sig = e->sig_ready ? e->d_sig : nullptr;
   c.damping = prm.damping;
   c.inv_n = 1.0 / V;
   c.fx_scale = static_cast<double>(V) * 1073741824.0;  // 2^30 per 1/N of rank
@@ -761,7 +766,6 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   fa.stats = e->d_stats;
   fa.bm = e->d_bm;
   fa.n_words = e->n_words;
-  fa.sig = e->d_sig;
   fa.val[0] = e->d_val[0];
   fa.val[1] = e->d_val[1];
   fa.outdeg = e->d_outdeg;
@@ -905,6 +909,15 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
       steps_before = e->h_ctl->step;
       GX_TRY(checkpoint(*e->h_ctl));
       if (e->h_ctl->done) break;
+      // Shard signatures are built the first time a step turns selective;
+      // until then selective steps sweep every shard.
+      if (!e->sig_ready && e->h_ctl->mode == MODE_SELECTIVE) {
+        GX_TRY(build_signatures(e));
+        const unsigned long long* sp = e->d_sig;
+        GX_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(e->d_ctl) + offsetof(Ctl, sig), &sp, sizeof(sp),
+                                cudaMemcpyHostToDevice, e->s_comp));
+        GX_CUDA(cudaStreamSynchronize(e->s_comp));
+      }
     }
     if (exec) cudaGraphExecDestroy(exec);
   } else {
@@ -1195,11 +1208,9 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   struct Scratch {
     cudaStream_t s;
     unsigned int* flag = nullptr;
-    int64_t* ebound = nullptr;
     ~Scratch() {
-      if (flag || ebound) cudaStreamSynchronize(s);
+      if (flag) cudaStreamSynchronize(s);
       dev_free(&flag);
-      dev_free(&ebound);
     }
   } scratch{e->s_copy};
   if (direct) {
@@ -1212,23 +1223,12 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
       GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
       GX_TRY(upload_async(e, e->d_outdeg, outdeg, sizeof(int32_t) * static_cast<size_t>(V), e->s_copy));
     }
-    // Behind the uploads: the load-time checks, then the shard signatures
-    // (whose kernel skips ids the checks will reject).
+    // Behind the uploads: the load-time checks.
     GX_TRY(dev_alloc(&scratch.flag, 1));
     GX_CUDA(cudaMemsetAsync(scratch.flag, 0, sizeof(unsigned int), e->s_copy));
     validate_csc_kernel<<<e->n_sm * 8, 256, 0, e->s_copy>>>(e->d_off, V, e->d_col, E, scratch.flag);
     GX_CUDA(cudaGetLastError());
-    e->shard_group = (P + 63) / 64;
-    GX_TRY(dev_alloc(&e->d_sig, static_cast<size_t>(V)));
-    GX_CUDA(cudaMemsetAsync(e->d_sig, 0, sizeof(unsigned long long) * V, e->s_copy));
-    std::vector<int64_t> ebound(static_cast<size_t>(P) + 1);
-    for (int32_t p = 0; p <= P; ++p) ebound[p] = off[bounds[p]];
-    GX_TRY(dev_alloc(&scratch.ebound, ebound.size()));
-    GX_CUDA(cudaMemcpyAsync(scratch.ebound, ebound.data(), sizeof(int64_t) * ebound.size(), cudaMemcpyHostToDevice,
-                            e->s_copy));
-    signature_all_kernel<<<e->n_sm * 8, 256, 0, e->s_copy>>>(e->d_sig, e->d_col, scratch.ebound, P, e->shard_group,
-                                                              V);
-    GX_CUDA(cudaGetLastError());
+    e->shard_group = (P + 63) / 64;  // signatures come later, at the first selective step
   }
   e->bounds.assign(bounds, bounds + P + 1);
   e->off.resize(static_cast<size_t>(V) + 1);

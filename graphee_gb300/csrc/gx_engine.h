@@ -185,6 +185,7 @@ struct gx_engine {
   uint32_t* d_bm = nullptr;
   int32_t n_words = 0;
   unsigned long long* d_sig = nullptr;
+  bool sig_ready = false;            // d_sig built (resident graphs build it at their first selective step)
   int4* d_frontier = nullptr;
   unsigned long long frontier_cap = 0;
   int64_t* d_ooff = nullptr;
@@ -249,6 +250,7 @@ struct gx_engine {
     gx::dev_free(&d_hticket);
     gx::dev_free(&d_bm);
     gx::dev_free(&d_sig);
+    sig_ready = false;
     gx::dev_free(&d_frontier);
     gx::dev_free(&d_ooff);
     gx::dev_free(&d_ocol);

@@ -47,6 +47,7 @@ struct Ctl {
   int async_mode;           // min apps: pull updates values in place (no buffer swap)
   int pad0;
   unsigned long long push_edge_limit;  // push when the frontier has at most this many out-edges
+  const unsigned long long* sig;       // per-vertex shard-group masks, or null until built
   double damping;
   double inv_n;             // 1.0 / N, as the reference computes it
   double fx_scale;          // fixed-point scale of resid_fx / dangl_fx
@@ -109,7 +110,6 @@ struct FinArgs {
   StepStats* stats;
   uint32_t* bm;
   int32_t n_words;
-  const unsigned long long* sig;  // per-vertex 64-bit mask of shard groups it feeds
   void* val[2];
   const int32_t* outdeg;
   int4* frontier;
@@ -792,7 +792,9 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
   // reference's selective steps it is chosen when the frontier's out-edges
   // are few enough to beat a full pull.
   const bool push_next = c.push_ok && (sel_next || c.front_edges <= c.push_edge_limit);
-  const bool want_mask = sel_next && !push_next && a.sig != nullptr;
+  // Without shard signatures (not built yet) a selective step sweeps every shard.
+  const unsigned long long* sig = c.sig;
+  const bool want_mask = sel_next && !push_next && sig != nullptr;
   const int nb = (c.mode == MODE_PUSH || c.async_mode) ? c.cur : (c.cur ^ 1);
   const T* newv = static_cast<const T*>(nb ? a.val[1] : a.val[0]);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -806,7 +808,7 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
       a.bm[w] = 0;
       act += __popc(word);
       if (want_mask) {
-        for (uint32_t x = word; x; x &= x - 1) mask |= a.sig[(w << 5) + __ffs(x) - 1];
+        for (uint32_t x = word; x; x &= x - 1) mask |= sig[(w << 5) + __ffs(x) - 1];
       }
     }
     if (push_next) {

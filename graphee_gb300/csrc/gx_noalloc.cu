@@ -167,7 +167,6 @@ extern "C" gx_status gx_pagerank_noalloc(const int64_t* d_off, const int32_t* d_
   fa.stats = s->stats;
   fa.bm = s->bm;
   fa.n_words = n_words;
-  fa.sig = nullptr;
   fa.val[0] = d_rank;
   fa.val[1] = s->val1;
   fa.outdeg = nullptr;
