@@ -7,10 +7,17 @@
 // N = the instance's vertex count) for up to pr_iters supersteps and then
 // its min-label CC (comp_cc, GraphMP/app/cc.cpp:20-75) to convergence, each
 // with GraphPS::run's stop rule per instance (GraphMP/system/GraphPS.h:383).
-// A CTA owns an instance at a time, so a superstep's barrier is a CTA
-// barrier; CTAs claim instances longest first.  Inside a CTA, warps sweep
-// 32-vertex tiles: lanes walk lists of up to `lane_max` edges alone (edge
-// order), longer lists are swept by the whole warp.
+// CTAs claim work slots longest instance first.  A small instance is one slot
+// and its superstep barrier a CTA barrier; an instance larger than about half
+// a CTA's fair share of the batch is split over a team of CTAs (one slot per
+// member, claimed consecutively), whose members sweep interleaved tiles and
+// meet at a global barrier after every superstep: an arrival counter and
+// triple-buffered change counts per instance, polled with a bounded spin (a
+// timeout raises an abort flag that every CTA honours, and the host reports
+// GX_ERR_TIMEOUT).  The launch holds no more CTAs than fit on the GPU at
+// once, so every member of a claimed team is running.  Inside a CTA, warps
+// sweep 32-vertex tiles: lanes walk lists of up to `lane_max` edges alone
+// (edge order), longer lists are swept by the whole warp.
 // Threads per CTA, lane_max and CTAs per SM come from the autotuner
 // (gx_batch_autotune), which times candidate schedules on the batch and
 // records the winner in a table file.
@@ -34,9 +41,13 @@ struct BatchArgs {
   const int32_t* col;
   const int32_t* outdeg;
   const int32_t* vbeg;      // n_inst + 1
-  const int32_t* order;     // claim order (longest first)
+  const int2* slots;        // claim order: (instance, member << 16 | team size), longest first
+  int32_t n_slots;
   int32_t n_inst;
   unsigned int* ctr;
+  unsigned int* team;       // per instance: arrivals, change counts [3]
+  unsigned int* abort;      // set when a team barrier times out
+  unsigned int spin_limit;
   float *pr0, *pr1;
   float *con0, *con1;
   int32_t *lab0, *lab1;
@@ -111,32 +122,92 @@ __device__ __forceinline__ void batch_vertex_lists(const BatchArgs& a, const flo
   }
 }
 
+// Barrier b of a team of `team` CTAs on instance state t[0..3]: adds this
+// CTA's change count to t[1 + b % 3] (member 0 first clears the slot barrier
+// b + 1 will use) and returns the team's total.  Every thread of the CTA
+// calls it.  Returns false when the wait timed out or another team aborted.
+__device__ bool team_barrier(const BatchArgs& a, unsigned int* t, int team, int member, int b, unsigned changed,
+                             unsigned* total) {
+  __shared__ unsigned s_tot;
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    if (member == 0) atomicExch(t + 1 + (b + 1) % 3, 0u);
+    if (changed) atomicAdd(t + 1 + b % 3, changed);
+    __threadfence();
+    atomicAdd(t, 1u);
+    const unsigned target = static_cast<unsigned>(b + 1) * static_cast<unsigned>(team);
+    volatile unsigned* arr = t;
+    volatile unsigned* ab = a.abort;
+    for (unsigned it = 0; *arr < target; ++it) {
+      if (*ab || it >= a.spin_limit) {
+        atomicExch(a.abort, 1u);
+        ok = 0;
+        break;
+      }
+      __nanosleep(64);
+    }
+    __threadfence();
+    s_tot = *reinterpret_cast<volatile unsigned*>(t + 1 + b % 3);
+    s_ok = ok;
+  }
+  __syncthreads();
+  *total = s_tot;
+  return s_ok != 0;
+}
+
 __global__ void batch_kernel(BatchArgs a) {
-  __shared__ int s_inst;
+  __shared__ int s_slot;
   __shared__ unsigned int s_changed;
+  __shared__ int s_next;  // next tile of this CTA's share, claimed by warps as they finish
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   for (;;) {
-    if (threadIdx.x == 0) s_inst = static_cast<int>(atomicAdd(a.ctr, 1u));
+    if (threadIdx.x == 0) s_slot = static_cast<int>(atomicAdd(a.ctr, 1u));
     __syncthreads();
-    const int slot = s_inst;
+    const int slot = s_slot;
     __syncthreads();
-    if (slot >= a.n_inst) break;
-    const int inst = a.order[slot];
+    if (slot >= a.n_slots) break;
+    if (*reinterpret_cast<volatile unsigned*>(a.abort)) break;
+    const int2 sl = a.slots[slot];
+    const int inst = sl.x, member = sl.y >> 16, team = sl.y & 0xffff;
+    unsigned int* tstate = a.team + 4 * static_cast<int64_t>(inst);
     const int32_t vb = a.vbeg[inst], ve = a.vbeg[inst + 1], n = ve - vb;
     const int tiles = (n + 31) / 32;
     const double inv_n = 1.0 / n;
+    const int vt0 = member * blockDim.x + threadIdx.x, vstride = blockDim.x * team;
+    int bar = 0;
+    // The barrier that ends a phase: a CTA barrier, or the team's.
+    auto sync_count = [&](unsigned mine, unsigned* total) -> bool {
+      if (team == 1) {
+        if (threadIdx.x == 0) s_changed = 0;
+        __syncthreads();
+        if (threadIdx.x == 0) s_next = 0;
+        if (lane == 0 && mine) atomicAdd(&s_changed, mine);
+        __syncthreads();
+        *total = s_changed;
+        __syncthreads();
+        return true;
+      }
+      if (threadIdx.x == 0) s_changed = 0;
+      __syncthreads();
+      if (threadIdx.x == 0) s_next = 0;
+      if (lane == 0 && mine) atomicAdd(&s_changed, mine);
+      __syncthreads();
+      const unsigned cta = s_changed;
+      return team_barrier(a, tstate, team, member, bar++, threadIdx.x == 0 ? cta : 0u, total);
+    };
+    unsigned tot = 0;
     // ---- PageRank ----
-    for (int v = vb + threadIdx.x; v < ve; v += blockDim.x) {
+    for (int v = vb + vt0; v < ve; v += vstride) {
       const float r0 = static_cast<float>(inv_n);
       const int32_t od = a.outdeg[v];
       a.pr0[v] = r0;
       a.con0[v] = r0 / static_cast<float>(od > 0 ? od : 1);
     }
-    __syncthreads();
+    if (!sync_count(0, &tot)) return;
     int cur = 0, step = 0;
     for (step = 0; step < a.pr_iters; ++step) {
-      if (threadIdx.x == 0) s_changed = 0;
-      __syncthreads();
       // Ternaries, not a[cur]: runtime indexing of a parameter array would
       // copy the parameter block to local memory.
       const float* con = cur ? a.con1 : a.con0;
@@ -144,7 +215,12 @@ __global__ void batch_kernel(BatchArgs a) {
       float* dst = cur ? a.pr0 : a.pr1;
       float* dcon = cur ? a.con0 : a.con1;
       unsigned changed = 0;
-      for (int t = wid; t < tiles; t += nw) {
+      for (;;) {
+        int k = 0;
+        if (lane == 0) k = atomicAdd(&s_next, 1);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        const int t = member + k * team;  // this CTA's tiles: member, member + team, ...
+        if (t >= tiles) break;
         const int v = vb + 32 * t + lane;
         const bool valid = v < ve;
         int64_t beg = 0, end = 0;
@@ -166,29 +242,29 @@ __global__ void batch_kernel(BatchArgs a) {
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) changed += __shfl_xor_sync(0xffffffffu, changed, o);
-      if (lane == 0 && changed) atomicAdd(&s_changed, changed);
-      __syncthreads();
+      if (!sync_count(changed, &tot)) return;
       cur ^= 1;
-      const unsigned ch = s_changed;
-      __syncthreads();
-      if (ch == 0 && step > 1) {
+      if (tot == 0 && step > 1) {
         ++step;
         break;
       }
     }
-    for (int v = vb + threadIdx.x; v < ve; v += blockDim.x) a.pr_out[v] = (cur ? a.pr1 : a.pr0)[v];
-    if (threadIdx.x == 0) a.pr_steps[inst] = step < a.pr_iters ? step : a.pr_iters;
+    for (int v = vb + vt0; v < ve; v += vstride) a.pr_out[v] = (cur ? a.pr1 : a.pr0)[v];
+    if (threadIdx.x == 0 && member == 0) a.pr_steps[inst] = step < a.pr_iters ? step : a.pr_iters;
     // ---- CC ----
-    for (int v = vb + threadIdx.x; v < ve; v += blockDim.x) a.lab0[v] = v - vb;
-    __syncthreads();
+    for (int v = vb + vt0; v < ve; v += vstride) a.lab0[v] = v - vb;
+    if (!sync_count(0, &tot)) return;
     cur = 0;
     for (step = 0; step < a.cc_max; ++step) {
-      if (threadIdx.x == 0) s_changed = 0;
-      __syncthreads();
       const int32_t* src = cur ? a.lab1 : a.lab0;
       int32_t* dst = cur ? a.lab0 : a.lab1;
       unsigned changed = 0;
-      for (int t = wid; t < tiles; t += nw) {
+      for (;;) {
+        int k = 0;
+        if (lane == 0) k = atomicAdd(&s_next, 1);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        const int t = member + k * team;
+        if (t >= tiles) break;
         const int v = vb + 32 * t + lane;
         const bool valid = v < ve;
         int64_t beg = 0, end = 0;
@@ -208,18 +284,15 @@ __global__ void batch_kernel(BatchArgs a) {
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) changed += __shfl_xor_sync(0xffffffffu, changed, o);
-      if (lane == 0 && changed) atomicAdd(&s_changed, changed);
-      __syncthreads();
+      if (!sync_count(changed, &tot)) return;
       cur ^= 1;
-      const unsigned ch = s_changed;
-      __syncthreads();
-      if (ch == 0 && step > 1) {
+      if (tot == 0 && step > 1) {
         ++step;
         break;
       }
     }
-    for (int v = vb + threadIdx.x; v < ve; v += blockDim.x) a.cc_out[v] = (cur ? a.lab1 : a.lab0)[v];
-    if (threadIdx.x == 0) a.cc_steps[inst] = step < a.cc_max ? step : a.cc_max;
+    for (int v = vb + vt0; v < ve; v += vstride) a.cc_out[v] = (cur ? a.lab1 : a.lab0)[v];
+    if (threadIdx.x == 0 && member == 0) a.cc_steps[inst] = step < a.cc_max ? step : a.cc_max;
     __syncthreads();
   }
 }
@@ -241,13 +314,20 @@ __global__ void batch_check_kernel(const int64_t* off, const int32_t* col, const
 }
 
 struct BatchDev {
-  int32_t *vbeg = nullptr, *order = nullptr, *lab0 = nullptr, *lab1 = nullptr, *cc_out = nullptr;
+  int32_t *vbeg = nullptr, *lab0 = nullptr, *lab1 = nullptr, *cc_out = nullptr;
   int32_t *pr_steps = nullptr, *cc_steps = nullptr;
   float *pr0 = nullptr, *pr1 = nullptr, *con0 = nullptr, *con1 = nullptr, *pr_out = nullptr;
   unsigned int* ctr = nullptr;
+  int2* slots = nullptr;
+  unsigned int* team = nullptr;     // 4 per instance
+  unsigned int* abort = nullptr;
+  std::vector<int32_t> order;       // instances, longest first
+  std::vector<int64_t> work;        // per instance: edges + vertices
   ~BatchDev() {
     dev_free(&vbeg);
-    dev_free(&order);
+    dev_free(&slots);
+    dev_free(&team);
+    dev_free(&abort);
     dev_free(&lab0);
     dev_free(&lab1);
     dev_free(&cc_out);
@@ -267,13 +347,17 @@ gx_status batch_prepare(gx_engine* e, int32_t n, const int32_t* vbeg, BatchDev& 
   if (vbeg[0] != 0 || vbeg[n] != V) return fail(GX_ERR_INVALID, "gx_batch: instance ranges must cover [0, V)");
   for (int32_t i = 0; i < n; ++i)
     if (vbeg[i + 1] <= vbeg[i]) return fail(GX_ERR_INVALID, "gx_batch: instance %d is empty or out of order", i);
-  std::vector<int32_t> order(n);
+  std::vector<int32_t>& order = d.order;
+  order.resize(n);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
     return e->off[vbeg[x + 1]] - e->off[vbeg[x]] > e->off[vbeg[y + 1]] - e->off[vbeg[y]];
   });
+  d.work.resize(n);
+  for (int32_t i = 0; i < n; ++i) d.work[i] = (e->off[vbeg[i + 1]] - e->off[vbeg[i]]) + (vbeg[i + 1] - vbeg[i]);
   GX_TRY(dev_alloc(&d.vbeg, static_cast<size_t>(n) + 1));
-  GX_TRY(dev_alloc(&d.order, static_cast<size_t>(n)));
+  GX_TRY(dev_alloc(&d.team, 4 * static_cast<size_t>(n)));
+  GX_TRY(dev_alloc(&d.abort, 1));
   GX_TRY(dev_alloc(&d.lab0, static_cast<size_t>(V)));
   GX_TRY(dev_alloc(&d.lab1, static_cast<size_t>(V)));
   GX_TRY(dev_alloc(&d.cc_out, static_cast<size_t>(V)));
@@ -286,7 +370,6 @@ gx_status batch_prepare(gx_engine* e, int32_t n, const int32_t* vbeg, BatchDev& 
   GX_TRY(dev_alloc(&d.cc_steps, static_cast<size_t>(n)));
   GX_TRY(dev_alloc(&d.ctr, 1));
   GX_CUDA(cudaMemcpy(d.vbeg, vbeg, sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice));
-  GX_CUDA(cudaMemcpy(d.order, order.data(), sizeof(int32_t) * n, cudaMemcpyHostToDevice));
   // Every edge must stay inside its instance (a block-diagonal CSC).
   GX_CUDA(cudaMemset(d.ctr, 0, sizeof(unsigned int)));
   batch_check_kernel<<<e->n_sm * 8, 256, 0, e->s_comp>>>(e->d_off, e->d_col, d.vbeg, n, V, d.ctr);
@@ -299,9 +382,11 @@ gx_status batch_prepare(gx_engine* e, int32_t n, const int32_t* vbeg, BatchDev& 
   a.col = e->d_col;
   a.outdeg = e->d_outdeg;
   a.vbeg = d.vbeg;
-  a.order = d.order;
   a.n_inst = n;
   a.ctr = d.ctr;
+  a.team = d.team;
+  a.abort = d.abort;
+  a.spin_limit = 1u << 24;  // polls of at least 64 ns: over a second
   a.pr0 = d.pr0;
   a.pr1 = d.pr1;
   a.con0 = d.con0;
@@ -315,16 +400,36 @@ gx_status batch_prepare(gx_engine* e, int32_t n, const int32_t* vbeg, BatchDev& 
   return GX_OK;
 }
 
-// One persistent launch (plus its cursor reset), captured as a CUDA graph.
-gx_status batch_launch(gx_engine* e, const BatchArgs& a, const gx_batch_tuning& t, float* ms) {
+// One persistent launch (plus its cursor and team-state resets), captured as
+// a CUDA graph.  The grid holds no more CTAs than are resident at once.
+gx_status batch_launch(gx_engine* e, BatchDev& d, BatchArgs& a, const gx_batch_tuning& t, float* ms) {
   cudaStream_t s = e->s_comp;
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, t.threads, 0);
-  const int blocks = std::max(1, std::min(per_sm, t.ctas_per_sm)) * e->n_sm;
+  if (per_sm < 1) return fail(GX_ERR_INVALID, "gx_batch: %d threads per CTA do not fit an SM", t.threads);
+  const int blocks = std::min(per_sm, t.ctas_per_sm) * e->n_sm;
+  // Work slots: an instance above half a CTA's fair share gets a team of up
+  // to 32 CTAs (never more than the grid).
+  int64_t total = 0;
+  for (int64_t w : d.work) total += w;
+  const int64_t share = std::max<int64_t>(1, total / (2 * static_cast<int64_t>(blocks)));
+  std::vector<int2> slots;
+  slots.reserve(d.order.size());
+  for (int32_t inst : d.order) {
+    const int team = static_cast<int>(std::min<int64_t>({(d.work[inst] + share - 1) / share, 32, blocks}));
+    for (int m = 0; m < std::max(team, 1); ++m) slots.push_back(make_int2(inst, (m << 16) | std::max(team, 1)));
+  }
+  dev_free(&d.slots);
+  GX_TRY(dev_alloc(&d.slots, slots.size()));
+  GX_CUDA(cudaMemcpy(d.slots, slots.data(), sizeof(int2) * slots.size(), cudaMemcpyHostToDevice));
+  a.slots = d.slots;
+  a.n_slots = static_cast<int32_t>(slots.size());
   cudaGraph_t graph;
   cudaGraphExec_t exec;
   GX_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   cudaMemsetAsync(a.ctr, 0, sizeof(unsigned int), s);
+  cudaMemsetAsync(a.team, 0, sizeof(unsigned int) * 4 * static_cast<size_t>(a.n_inst), s);
+  cudaMemsetAsync(a.abort, 0, sizeof(unsigned int), s);
   batch_kernel<<<blocks, t.threads, 0, s>>>(a);
   GX_CUDA(cudaStreamEndCapture(s, &graph));
   cudaError_t err = cudaGraphInstantiate(&exec, graph, 0);
@@ -343,6 +448,9 @@ gx_status batch_launch(gx_engine* e, const BatchArgs& a, const gx_batch_tuning& 
   cudaEventDestroy(e1);
   cudaGraphExecDestroy(exec);
   if (err != cudaSuccess) return fail(GX_ERR_CUDA, "gx_batch: run failed: %s", cudaGetErrorString(err));
+  unsigned int aborted = 0;
+  GX_CUDA(cudaMemcpy(&aborted, a.abort, sizeof(aborted), cudaMemcpyDeviceToHost));
+  if (aborted) return fail(GX_ERR_TIMEOUT, "gx_batch: a CTA team barrier timed out");
   *ms = t_ms;
   return GX_OK;
 }
@@ -384,7 +492,7 @@ gx_status gx_batch_run(gx_engine* e, int32_t n_inst, const int32_t* inst_vbegin,
   a.lane_max = t.lane_max;
   a.damping = damping;
   float ms = 0;
-  GX_TRY(batch_launch(e, a, t, &ms));
+  GX_TRY(batch_launch(e, d, a, t, &ms));
   const int32_t V = e->V;
   if (pr_out) GX_CUDA(cudaMemcpy(pr_out, d.pr_out, sizeof(float) * V, cudaMemcpyDeviceToHost));
   if (cc_out) GX_CUDA(cudaMemcpy(cc_out, d.cc_out, sizeof(int32_t) * V, cudaMemcpyDeviceToHost));
@@ -431,8 +539,8 @@ gx_status gx_batch_autotune(gx_engine* e, int32_t n_inst, const int32_t* inst_vb
         gx_batch_tuning t{th, lm, cp};
         a.lane_max = lm;
         float ms = 0, ms2 = 0;
-        GX_TRY(batch_launch(e, a, t, &ms));   // warm
-        GX_TRY(batch_launch(e, a, t, &ms2));
+        GX_TRY(batch_launch(e, d, a, t, &ms));   // warm
+        GX_TRY(batch_launch(e, d, a, t, &ms2));
         ms = std::min(ms, ms2);
         char buf[160];
         snprintf(buf, sizeof(buf), "{\"threads\": %d, \"lane_max\": %d, \"ctas_per_sm\": %d, \"ms\": %.4f}", th, lm, cp,
