@@ -111,8 +111,12 @@ __global__ void __launch_bounds__(256, 3) mlp_features_kernel(const int64_t* off
                                                            float* feat, double* part_resid) {
   __shared__ double s_red[8];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const double invn = 1.0 / V;
-  double resid = 0;
+  // Per-vertex arithmetic is FP32 (FP64 is slow on this part): the uniform
+  // start's first-step residual term |r1 - 1/N| = d/N |sum_inv + D - 1| is
+  // summed per thread in FP32 (a few hundred terms) and across threads in FP64.
+  const float invn_f = static_cast<float>(1.0 / V), d_f = static_cast<float>(damping);
+  const float dang_f = static_cast<float>(dangling0);
+  float resid_f = 0.f;
   // The engine's work units (edge-capped tiles of consecutive vertices),
   // claimed dynamically; heavy chunks belong to mlp_heavy_features_kernel.
   for (int u = 0;; ++u) {
@@ -178,11 +182,11 @@ __global__ void __launch_bounds__(256, 3) mlp_features_kernel(const int64_t* off
       const int32_t od = outdeg[v];
       float4* fo = reinterpret_cast<float4*>(feat + static_cast<size_t>(v) * kFeatStride);
       fo[0] = make_float4(log1pf(deg), log1pf(static_cast<float>(od)), deg > 0 ? f.sum_g / deg : 0.f, f.max_g);
-      fo[1] = make_float4(static_cast<float>(log1p(static_cast<double>(f.sum_in))), od == 0 ? 1.f : 0.f, 0.f, 0.f);
-      const double r1 = (1.0 - damping) * invn + damping * (f.sum_inv * invn + dangling0 * invn);
-      resid += fabs(r1 - invn);
+      fo[1] = make_float4(log1pf(f.sum_in), od == 0 ? 1.f : 0.f, 0.f, 0.f);
+      resid_f += d_f * invn_f * fabsf(f.sum_inv + dang_f - 1.f);
     }
   }
+  double resid = resid_f;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) resid += __shfl_xor_sync(0xffffffffu, resid, o);
   if (lane == 0) s_red[wid] = resid;
@@ -243,10 +247,9 @@ __global__ void __launch_bounds__(256) mlp_heavy_features_kernel(const int64_t* 
       const int32_t od = outdeg[v];
       float4* fo = reinterpret_cast<float4*>(feat + static_cast<size_t>(v) * kFeatStride);
       fo[0] = make_float4(log1pf(deg), log1pf(static_cast<float>(od)), deg > 0 ? f.sum_g / deg : 0.f, f.max_g);
-      fo[1] = make_float4(static_cast<float>(log1p(static_cast<double>(f.sum_in))), od == 0 ? 1.f : 0.f, 0.f, 0.f);
+      fo[1] = make_float4(log1pf(f.sum_in), od == 0 ? 1.f : 0.f, 0.f, 0.f);
       const double invn = 1.0 / V;
-      const double r1 = (1.0 - damping) * invn + damping * (f.sum_inv * invn + dangling0 * invn);
-      part_resid[i] = fabs(r1 - invn);
+      part_resid[i] = damping * invn * fabs(static_cast<double>(f.sum_inv) + dangling0 - 1.0);
     }
     __syncthreads();
   }
