@@ -14,6 +14,7 @@
 //     shared memory is searched in place in global memory.
 // Counts are exact (64-bit integer sums).
 #include <cuda_runtime.h>
+#include <omp.h>
 
 #include <algorithm>
 #include <chrono>
@@ -229,22 +230,41 @@ extern "C" gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_sta
   std::vector<int32_t> cnt(V);
   GX_CUDA(cudaMemcpyAsync(cnt.data(), b.cnt, sizeof(int32_t) * V, cudaMemcpyDeviceToHost, s));
   GX_CUDA(cudaStreamSynchronize(s));
+  // Prefix sums and the claim order on the host threads: each thread scans
+  // and bins a contiguous block of vertices; blocks are joined in order.
+  const int nt = std::max(1, omp_get_max_threads());
   std::vector<int64_t> doff(static_cast<size_t>(V) + 1, 0);
-  for (int32_t v = 0; v < V; ++v) doff[v + 1] = doff[v] + cnt[v];
-  const int64_t m = doff[V];
-  std::vector<std::vector<int32_t>> bins(33);
-  std::vector<int32_t> big;
-  for (int32_t v = 0; v < V; ++v) {
-    if (cnt[v] < 2) continue;  // no pair of out-neighbours, no triangle
-    if (cnt[v] > kWarpList) {
-      big.push_back(v);
-      continue;
+  std::vector<int64_t> part(static_cast<size_t>(nt) + 1, 0);
+  std::vector<std::vector<std::vector<int32_t>>> tbins(nt, std::vector<std::vector<int32_t>>(34));
+#pragma omp parallel num_threads(nt)
+  {
+    const int t = omp_get_thread_num();
+    const int32_t lo = static_cast<int32_t>(static_cast<int64_t>(V) * t / nt);
+    const int32_t hi = static_cast<int32_t>(static_cast<int64_t>(V) * (t + 1) / nt);
+    int64_t run = 0;
+    for (int32_t v = lo; v < hi; ++v) {
+      run += cnt[v];
+      if (cnt[v] < 2) continue;  // no pair of out-neighbours, no triangle
+      tbins[t][cnt[v] > kWarpList ? 33 : 31 - __builtin_clz(static_cast<unsigned>(cnt[v]))].push_back(v);
     }
-    bins[31 - __builtin_clz(static_cast<unsigned>(cnt[v]))].push_back(v);
+    part[t + 1] = run;
+#pragma omp barrier
+#pragma omp single
+    for (int i = 0; i < nt; ++i) part[i + 1] += part[i];
+    int64_t acc = part[t];
+    for (int32_t v = lo; v < hi; ++v) {
+      doff[v] = acc;
+      acc += cnt[v];
+    }
   }
-  std::sort(big.begin(), big.end(), [&](int32_t a, int32_t c) { return cnt[a] > cnt[c]; });
+  doff[V] = part[nt];
+  const int64_t m = doff[V];
+  std::vector<int32_t> big;
+  for (int t = 0; t < nt; ++t) big.insert(big.end(), tbins[t][33].begin(), tbins[t][33].end());
+  std::sort(big.begin(), big.end(), [&](int32_t a, int32_t c) { return cnt[a] > cnt[c] || (cnt[a] == cnt[c] && a < c); });
   std::vector<int32_t> order(big);
-  for (int k = 32; k >= 0; --k) order.insert(order.end(), bins[k].begin(), bins[k].end());
+  for (int k = 32; k >= 0; --k)
+    for (int t = 0; t < nt; ++t) order.insert(order.end(), tbins[t][k].begin(), tbins[t][k].end());
   const int32_t n_big = static_cast<int32_t>(big.size());
   const int32_t n_small = static_cast<int32_t>(order.size()) - n_big;
   GX_TRY(dev_alloc(&b.doff, static_cast<size_t>(V) + 1));
@@ -256,10 +276,18 @@ extern "C" gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_sta
   tc_fill_kernel<<<grid, 256, 0, s>>>(e->d_off, e->d_col, b.deg, V, b.doff, b.dcol);
   GX_CUDA(cudaMemsetAsync(b.out, 0, 2 * sizeof(unsigned long long), s));
   GX_CUDA(cudaMemsetAsync(b.ctr, 0, sizeof(unsigned int), s));
+  // The long lists run on the copy stream beside the warp kernel, so the
+  // few CTAs they need do not hold the rest of the GPU idle.
+  cudaEvent_t filled = nullptr, big_done = nullptr;
   if (n_big > 0) {
+    GX_CUDA(cudaEventCreateWithFlags(&filled, cudaEventDisableTiming));
+    GX_CUDA(cudaEventCreateWithFlags(&big_done, cudaEventDisableTiming));
+    GX_CUDA(cudaEventRecord(filled, s));
+    GX_CUDA(cudaStreamWaitEvent(e->s_copy, filled, 0));
     const size_t smem = sizeof(int32_t) * kCtaList;
     GX_CUDA(cudaFuncSetAttribute(tc_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    tc_cta_kernel<<<std::min(n_big, e->n_sm), kTcThreads, smem, s>>>(b.doff, b.dcol, b.order, n_big, b.out);
+    tc_cta_kernel<<<std::min(n_big, e->n_sm), kTcThreads, smem, e->s_copy>>>(b.doff, b.dcol, b.order, n_big, b.out);
+    GX_CUDA(cudaEventRecord(big_done, e->s_copy));
   }
   if (n_small > 0) {
     int per_sm = 0;
@@ -268,6 +296,11 @@ extern "C" gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_sta
                                                                         b.ctr, b.out);
   }
   GX_CUDA(cudaGetLastError());
+  if (big_done) {
+    GX_CUDA(cudaStreamWaitEvent(s, big_done, 0));
+    cudaEventDestroy(filled);
+    cudaEventDestroy(big_done);
+  }
   unsigned long long res[2] = {0, 0};
   GX_CUDA(cudaMemcpyAsync(res, b.out, sizeof(res), cudaMemcpyDeviceToHost, s));
   GX_CUDA(cudaEventRecord(ev1, s));
