@@ -3,18 +3,20 @@
 //
 // HBM layout (all-resident case):
 //   off     int64[V+1]   global CSC offsets (the shards' indptr, rebased)
-//   col     int32[E+4]   source ids, shards laid end to end (the shards' indices)
-//   w       uint32[E+4]  SSSP weights aligned with col (optional)
+//   col     int32[E+8]   source ids, shards laid end to end (the shards' indices)
+//   w       uint32[E+8]  SSSP weights aligned with col (optional)
 //   outdeg  int32[V]     vertexout.npy
 //   val     T[2][V]      Msg / MsgNew as a double buffer (swap instead of copy)
 //   con     f32[2][V]    PageRank contributions Msg[u]/outdeg[u]
 //   units   int2[U]      warp work units, unit_shard int32[U]
 //   bm      u32[V/32+2]  next-frontier bitmap; frontier int4[V+E/256+1] (push only)
-//   sig     u64[V]       per-vertex shard-group mask (selective scheduling)
+//   sig     u64[V]       per-vertex shard-group mask (selective scheduling),
+//                        built at the first selective step
 //   ooff/ocol/ow         out-edge CSR for sparse push steps (SSSP/CC)
 // With a shard-cache budget, only the shards that fit stay in HBM; the others
 // are kept in pinned host memory and streamed per step through a ring of
-// device slots on a copy stream (the GPU form of load_edge, Global.h:129-255).
+// device slots on a copy stream (the GPU form of load_edge, Global.h:129-255),
+// compressed when that saves 15% of their bytes (encode_streamed).
 #include <cuda_runtime.h>
 #include <omp.h>
 
