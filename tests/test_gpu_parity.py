@@ -379,3 +379,23 @@ def test_load_rejects_bad_csc(budget):
         assert ei.value.status == gx.GX_ERR_INVALID
         e.load(g)                      # the engine is still usable
         assert e.run(gx.APP_CC, 100)["iterations"] > 0
+
+
+def test_selective_steps_skip_shards_and_keep_values():
+    """On a path the SSSP frontier is one vertex per step, far below BF_THRE:
+    with push steps off, every step after the first few is selective, and
+    the shard-group masks (built at the first selective step) leave all but
+    one or two shards idle.  Values and per-step counts stay the reference's."""
+    V = 4096
+    src = np.arange(V - 1, dtype=np.int32)
+    off, col = gx.build_csc(V, src, src + 1)
+    g = gx.Graph(V, off, col, None, 16)
+    ref, ch, _ = O.run(O.SSSP, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 5000, source=0)
+    e = engine_for(g, push_sparse=0)
+    st = e.run(gx.APP_SSSP, 5000, source=0)
+    assert np.array_equal(e.values(), ref)
+    assert np.array_equal(run_changed(e, st["iterations"]), ch)
+    sel = [e.iter_stats(i) for i in range(st["iterations"]) if e.iter_stats(i)["mode"] == 1]
+    assert len(sel) > V // 2
+    assert sum(m["shards_active"] <= 2 for m in sel) > len(sel) // 2
+    e.close()
