@@ -399,3 +399,19 @@ def test_selective_steps_skip_shards_and_keep_values():
     assert len(sel) > V // 2
     assert sum(m["shards_active"] <= 2 for m in sel) > len(sel) // 2
     e.close()
+
+
+@pytest.mark.parametrize("budget", [-1, 0])
+def test_graph_without_edges(budget):
+    """No edges at all (every shard empty): the apps still follow the
+    reference's loop and stop rule, resident or with a zero budget."""
+    V, P = 100, 4
+    g = gx.Graph(V, np.zeros(V + 1, np.int64), np.zeros(0, np.int32), None, P)
+    for app, kw, oapp in [(gx.APP_PAGERANK_REF, {}, O.PAGERANK_REF), (gx.APP_SSSP, {"source": 0}, O.SSSP),
+                          (gx.APP_CC, {}, O.CC)]:
+        ref, ch, _ = O.run(oapp, V, P, g.bounds, g.off, g.col, g.outdeg, 50, **kw)
+        with gx.Engine(cache_budget_bytes=budget) as e:
+            e.load(g)
+            st = e.run(app, 50, **kw)
+            assert np.array_equal(e.values().view(np.uint32), ref.view(np.uint32)), app
+            assert np.array_equal(run_changed(e, st["iterations"]), ch), app
