@@ -29,6 +29,7 @@ import subprocess
 import sys
 import tempfile
 import time
+from contextlib import nullcontext as _nullcontext
 from pathlib import Path
 
 import numpy as np
@@ -57,7 +58,7 @@ def aggregate(ms_step: float, units_per_rank: float, dist=None, device=None):
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gx", choices=["gx", "reference"])
     ap.add_argument("--scale", type=int, default=24)
@@ -65,7 +66,7 @@ def parse():
     ap.add_argument("--iters", type=int, default=20)
     ap.add_argument("--cpu-iters", type=int, default=2, help="PageRank supersteps in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-sssp", action="store_true", help="skip the SSSP keys of the default run")
     ap.add_argument("--workload", default="pagerank",
                     choices=["pagerank", "cc_tc", "stream", "batch", "ppr", "warm"],
@@ -78,22 +79,29 @@ def dist_env():
 
 
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+    """nvidia-smi clocks / throttle reasons, sampled every 100 ms from before
+    the warm-up to the end of the timed regions.  Each sample carries
+    nvidia-smi's own timestamp; the summary keeps the samples taken inside the
+    timed regions (marked with window())."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    REASONS = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
 
     def __init__(self, gpu: int):
         self.gpu = gpu
         self.proc = None
-        self.path = Path(tempfile.mkstemp(suffix=".csv")[1])
+        self.windows = []
+        fd, name = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        self.path = Path(name)
 
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
         return self
@@ -106,28 +114,50 @@ class ClockSampler:
             except subprocess.TimeoutExpired:
                 self.proc.kill()
 
-    def summary(self):
-        if self.proc is None or not self.path.exists():
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        sm, smax, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    class _Window:
+        def __init__(self, owner):
+            self.owner = owner
+
+        def __enter__(self):
+            self.t0 = time.time()
+
+        def __exit__(self, *exc):
+            self.owner.windows.append((self.t0, time.time()))
+
+    def window(self):
+        return ClockSampler._Window(self)
+
+    def _samples(self):
+        from datetime import datetime
+        out = []
         for line in self.path.read_text().splitlines():
             parts = [x.strip() for x in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                sm.append(float(parts[1]))
-                smax.append(float(parts[2]))
+                ts = datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                sm, smax = float(parts[2]), float(parts[3])
             except ValueError:
                 continue
-            for name, val in zip(names, parts[5:9]):
-                if val.lower() == "active":
-                    reasons.add(name)
+            active = {n for n, v in zip(self.REASONS, parts[6:10]) if v.lower() == "active"}
+            out.append((ts, sm, smax, active))
+        return out
+
+    def summary(self):
+        samples = self._samples() if self.proc is not None and self.path.exists() else []
         self.path.unlink(missing_ok=True)
-        if not sm:
+        inside = [x for x in samples if any(a <= x[0] <= b for a, b in self.windows)]
+        where = "timed regions"
+        if not inside and self.windows:
+            # Timed regions shorter than the sampling period: the samples
+            # from the warm-up on (the GPU under the same load) stand in.
+            inside = [x for x in samples if x[0] >= self.windows[0][0] - 2.0]
+            where = "warm-up and timed regions (timed regions shorter than the 100 ms period)"
+        if not inside:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
-        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
-                "samples": len(sm)}
+        reasons = set().union(*(x[3] for x in inside))
+        return {"sm_mhz": statistics.median(x[1] for x in inside), "sm_max_mhz": max(x[2] for x in inside),
+                "reasons": sorted(reasons), "samples": len(inside), "sampled": where}
 
 
 def measured_peak_hbm():
@@ -281,11 +311,12 @@ def run_gx(args, rank, local_rank, world):
     g, build_s = build_graph(args, device=local_rank)
     eng = gx.Engine(device=local_rank)
     eng.load(g)
+    clk = ClockSampler(local_rank).__enter__()
     for _ in range(args.warmup):
         eng.run(gx.APP_PAGERANK_REF, args.iters)
 
     barrier()
-    with ClockSampler(local_rank) as clk:
+    with clk.window():
         t0 = time.perf_counter()
         dev_ms = 0.0
         launches = 0
@@ -297,7 +328,6 @@ def run_gx(args, rank, local_rank, world):
             iters_done += st["iterations"]
         barrier()
         wall = time.perf_counter() - t0
-    clocks = clk.summary()
     edges_per_step = g.E * args.iters
     ms_step, eps = aggregate(dev_ms / args.steps, float(edges_per_step), dist, "cuda")
     value = eps / 1e9
@@ -323,14 +353,17 @@ def run_gx(args, rank, local_rank, world):
     e2 = gx.Engine(device=local_rank)
     for i in range(args.e2e_steps + 1):
         barrier()
-        t1 = time.perf_counter()
-        e2.load(g)
-        e2.run(gx.APP_PAGERANK_REF, args.iters)
-        vals = e2.values(out=result)
-        torch.cuda.synchronize()
-        if i > 0:
-            e2e_s.append(time.perf_counter() - t1)
+        with clk.window() if i > 0 else _nullcontext():
+            t1 = time.perf_counter()
+            e2.load(g)
+            e2.run(gx.APP_PAGERANK_REF, args.iters)
+            vals = e2.values(out=result)
+            torch.cuda.synchronize()
+            if i > 0:
+                e2e_s.append(time.perf_counter() - t1)
     e2.close()
+    clk.__exit__(None, None, None)
+    clocks = clk.summary()
     e2e_step, e2e_eps = aggregate(sum(e2e_s) / len(e2e_s) * 1000, float(edges_per_step), dist, "cuda")
     e2e_step /= 1000
     h2d = 4 * g.E + 8 * (g.V + 1) + 4 * g.V
