@@ -1,7 +1,7 @@
 """FP64 restatement of the warm-start MLP (forward, loss, backward) and of
 its input features.
 
-TEST INFRASTRUCTURE ONLY: the checker for the GPU training kernels'
+TEST INFRASTRUCTURE ONLY: the correctness reference for the GPU training kernels'
 gradients and the feature kernel.  Same parameter layout as the library:
 W1[64][6], b1[64], W2[64][64], b2[64], w3[64], b3; forward uses W1, W2, w3
 rounded to BF16 (round to nearest even), biases in full precision.

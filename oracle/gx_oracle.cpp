@@ -1,6 +1,6 @@
 // CPU restatement of GraphMP's engine loop and vertex programs.
 //
-// TEST INFRASTRUCTURE ONLY: the checker for the CUDA path and the timed CPU
+// TEST INFRASTRUCTURE ONLY: the correctness reference for the CUDA path and the timed CPU
 // baseline.  Never linked into the product.  Built with -ffp-contract=off so
 // the float PageRank matches the reference bit for bit on x86 and on Arm.
 //

@@ -1,7 +1,7 @@
 /*
  * gx_oracle.h — CPU restatement of GraphMP's engine and vertex programs.
  *
- * TEST INFRASTRUCTURE ONLY.  The checker for the CUDA path and the timed CPU
+ * TEST INFRASTRUCTURE ONLY.  The correctness reference for the CUDA path and the timed CPU
  * baseline ("port"); the product never links, loads or calls it.  Pinned
  * against outputs of the reference's own apps (oracle/_ref, built by
  * oracle/Makefile) stored under tests/golden/.

@@ -1,7 +1,7 @@
 """ctypes wrapper of the oracle (oracle/gx_oracle.cpp).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
-the checker, and by bench.py's CPU-baseline leg.  The product path never
+the correctness reference, and by bench.py's CPU-baseline leg.  The product path never
 imports it.  Pinned against the reference's own outputs in tests/golden/.
 """
 from __future__ import annotations

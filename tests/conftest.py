@@ -11,7 +11,7 @@ GOLDEN = Path(__file__).resolve().parent / "golden"
 
 
 def pytest_configure(config):
-    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs on the GB300 box)")
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
 @pytest.fixture(scope="session")
