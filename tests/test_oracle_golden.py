@@ -92,6 +92,30 @@ def test_pagerank_std_sums_to_one():
     assert np.abs(fix - vals).max() < 1e-12
 
 
+def test_ppr_converges_to_linear_solve():
+    """Personalized PageRank (no reference counterpart): after enough steps
+    of R <- c S + (1-c) A^T D^-1 R each column equals the solution of
+    (I - (1-c) A^T D^-1) r = c e_source, solved here by scipy."""
+    sp = pytest.importorskip("scipy.sparse")
+    spl = pytest.importorskip("scipy.sparse.linalg")
+    import graphee_gb300 as gx
+    g = gx.rmat_graph(10, 8, seed=6, P=4)
+    c = 0.15
+    src = np.array([0, 3, 17, g.V - 1], np.int32)
+    R = O.ppr(g.V, g.off, g.col, g.outdeg, src, 300, c)
+    # M[v, u] = 1/outdeg(u) for every edge u -> v (rows = destinations, the CSC's columns)
+    inv = 1.0 / np.maximum(np.asarray(g.outdeg, np.float64), 1)
+    M = sp.csr_matrix((inv[g.col], np.asarray(g.col, np.int64), np.asarray(g.off, np.int64)), shape=(g.V, g.V))
+    A = (sp.identity(g.V, format="csc") - (1 - c) * M).tocsc()
+    for j, s in enumerate(src):
+        rhs = np.zeros(g.V)
+        rhs[s] = c
+        x = spl.spsolve(A, rhs)
+        assert np.abs(R[:, j] - x).max() <= 1e-12 * max(1.0, x.max()), j
+    # dangling mass leaves the system, so each column sums to at most 1
+    assert (R.sum(0) <= 1 + 1e-12).all() and (R >= 0).all()
+
+
 def test_triangles_match_networkx():
     nx = pytest.importorskip("networkx")
     import graphee_gb300 as gx
