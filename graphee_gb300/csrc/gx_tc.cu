@@ -8,10 +8,14 @@
 //  2. build the oriented adjacency N+(u) with warp-ballot compaction, which
 //     keeps the ascending id order of the input lists;
 //  3. count sum over u, v in N+(u) of |N+(u) ∩ N+(v)|: a warp stages N+(u)
-//     in shared memory and its lanes binary-search every w of N+(v) in it.
+//     in shared memory with an 8192-bit filter of its ids; its lanes test
+//     every w of N+(v) against the filter, and only the ids that pass are
+//     queued and binary-searched in the staged list, 32 at a time.
 //     Vertices are claimed in descending |N+(u)| order; lists too long for
-//     a warp's slice get a whole CTA, and the rare list beyond the CTA's
-//     shared memory is searched in place in global memory.
+//     a warp's slice get a whole CTA (a 2^16-bit filter, warps splitting
+//     N+(u)), whose shared memory is sized to the longest such list so it
+//     runs beside the warp kernel; the rare list beyond kCtaList entries is
+//     searched in place in global memory.
 // Counts are exact (64-bit integer sums).
 #include <cuda_runtime.h>
 #include <omp.h>
@@ -93,15 +97,56 @@ __device__ __forceinline__ bool tc_search(const int32_t* list, int n, int32_t w)
   return lo < n && list[lo] == w;
 }
 
-// Lanes of one warp intersect N+(v) (global) with the staged list.
-__device__ __forceinline__ unsigned long long tc_probe(const int64_t* doff, const int32_t* dcol, const int32_t* list,
-                                                       int n, int32_t v, int lane, int stride,
-                                                       unsigned long long* work) {
-  const int64_t vb = doff[v], ve = doff[v + 1];
-  unsigned long long c = 0;
-  for (int64_t j = vb + lane; j < ve; j += stride) c += tc_search(list, n, dcol[j]);
-  if (lane == 0) *work += ve - vb;
-  return c;
+// Bit filter of a staged list: bit h(w) is set for every w of the list, so a
+// clear bit proves w absent.  Multiplicative hashing spreads R-MAT's
+// structured ids over the 2^kFilterBits bits.
+constexpr int kFilterBits = 13;                          // a warp's list (<= 1024 ids)
+constexpr int kFilterWords = (1 << kFilterBits) / 32;
+constexpr int kCtaFilterBits = 16;                       // a CTA's list (> 1024 ids)
+constexpr int kCtaFilterWords = (1 << kCtaFilterBits) / 32;
+template <int BITS>
+__device__ __forceinline__ uint32_t tc_hash(int32_t w) {
+  return (static_cast<uint32_t>(w) * 2654435761u) >> (32 - BITS);
+}
+
+// Lanes of one warp test every w of N+(v) against the staged list's bit
+// filter.  Most probes miss (about 90% on R-MAT) and the filter rejects all
+// but 1-2% of those with one shared-memory load; the ids that pass are
+// appended to the warp's queue (ballot + prefix) and binary-searched 32 at a
+// time, so the searches run with every lane busy.  qn (warp-uniform) is the
+// queue's fill, below 32 between calls.  N+(v) lies at dcol[vb, vb + len);
+// each round's id is loaded one round ahead, so the load's latency overlaps
+// the current round's filter test.
+template <int BITS>
+__device__ __forceinline__ void tc_probe_filtered(const int32_t* __restrict__ dcol, int64_t vb, int len,
+                                                  const int32_t* list, int n, const uint32_t* bits, int32_t* q,
+                                                  int& qn, int lane, unsigned long long& cnt,
+                                                  unsigned long long& work) {
+  const int32_t* nv = dcol + vb;
+  if (lane == 0) work += static_cast<unsigned long long>(len);
+  const unsigned below = (1u << lane) - 1u;
+  int32_t w_next = lane < len ? nv[lane] : 0;
+  for (int base = 0; base < len; base += 32) {
+    const int j = base + lane;
+    const int32_t w = w_next;
+    if (j + 32 < len) w_next = nv[j + 32];
+    bool pass = false;
+    if (j < len) {
+      const uint32_t h = tc_hash<BITS>(w);
+      pass = (bits[h >> 5] >> (h & 31)) & 1u;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, pass);
+    if (pass) q[qn + __popc(m & below)] = w;
+    qn += __popc(m);
+    if (qn >= 32) {
+      __syncwarp();
+      cnt += tc_search(list, n, q[lane]);
+      __syncwarp();
+      if (lane < qn - 32) q[lane] = q[32 + lane];
+      qn -= 32;
+    }
+  }
+  __syncwarp();
 }
 
 // Warp per vertex; vertices in `order` (descending |N+|) with |N+| <= kWarpList.
@@ -109,9 +154,13 @@ __global__ void __launch_bounds__(kTcThreads) tc_warp_kernel(const int64_t* doff
                                                              const int32_t* order, int32_t n_order, unsigned int* ctr,
                                                              unsigned long long* out) {
   __shared__ int32_t s_list[kTcWarps][kWarpList];
+  __shared__ uint32_t s_bits[kTcWarps][kFilterWords];
+  __shared__ int32_t s_q[kTcWarps][64];
   __shared__ unsigned long long s_red[2][kTcWarps];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   int32_t* list = s_list[wid];
+  uint32_t* bits = s_bits[wid];
+  int32_t* q = s_q[wid];
   unsigned long long cnt = 0, work = 0;
   for (;;) {
     int i0 = 0;
@@ -123,9 +172,30 @@ __global__ void __launch_bounds__(kTcThreads) tc_warp_kernel(const int64_t* doff
       const int32_t u = order[i];
       const int64_t b = doff[u];
       const int n = static_cast<int>(doff[u + 1] - b);
-      for (int k = lane; k < n; k += 32) list[k] = dcol[b + k];
+      for (int k = lane; k < kFilterWords; k += 32) bits[k] = 0u;
       __syncwarp();
-      for (int k = 0; k < n; ++k) cnt += tc_probe(doff, dcol, list, n, list[k], lane, 32, &work);
+      for (int k = lane; k < n; k += 32) {
+        const int32_t x = dcol[b + k];
+        list[k] = x;
+        const uint32_t h = tc_hash<kFilterBits>(x);
+        atomicOr(&bits[h >> 5], 1u << (h & 31));
+      }
+      __syncwarp();
+      int qn = 0;
+      // Offsets of N+(v) for the next v are loaded while this one is probed.
+      int64_t vb = doff[list[0]], ve = doff[list[0] + 1];
+      for (int k = 0; k < n; ++k) {
+        int64_t nb = 0, ne = 0;
+        if (k + 1 < n) {
+          nb = doff[list[k + 1]];
+          ne = doff[list[k + 1] + 1];
+        }
+        tc_probe_filtered<kFilterBits>(dcol, vb, static_cast<int>(ve - vb), list, n, bits, q, qn, lane, cnt, work);
+        vb = nb;
+        ve = ne;
+      }
+      // The queue's rest belongs to this list: searched before the next is staged.
+      if (lane < qn) cnt += tc_search(list, n, q[lane]);
       __syncwarp();
     }
   }
@@ -148,23 +218,48 @@ __global__ void __launch_bounds__(kTcThreads) tc_warp_kernel(const int64_t* doff
 
 // CTA per vertex for |N+(u)| > kWarpList: the list is staged in dynamic
 // shared memory when it fits, else searched where it lies.
+// Dynamic shared memory: the 2^16-bit filter, the warps' queues, then room
+// for `cap` list entries (the longest list of the launch, at most kCtaList).
+// Vertices are claimed one at a time from ctr; warps split N+(u) and probe
+// through the filter like the warp kernel.
 __global__ void __launch_bounds__(kTcThreads) tc_cta_kernel(const int64_t* doff, const int32_t* dcol,
-                                                            const int32_t* order, int32_t n_order,
-                                                            unsigned long long* out) {
-  extern __shared__ int32_t s_big[];
+                                                            const int32_t* order, int32_t n_order, int cap,
+                                                            unsigned int* ctr, unsigned long long* out) {
+  extern __shared__ uint32_t s_dyn[];
+  uint32_t* bits = s_dyn;
+  int32_t* q = reinterpret_cast<int32_t*>(s_dyn + kCtaFilterWords) + 64 * (threadIdx.x >> 5);
+  int32_t* s_big = reinterpret_cast<int32_t*>(s_dyn + kCtaFilterWords) + 64 * kTcWarps;
   __shared__ unsigned long long s_red[2][kTcWarps];
+  __shared__ int s_i;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   unsigned long long cnt = 0, work = 0;
-  for (int i = blockIdx.x; i < n_order; i += gridDim.x) {
+  for (;;) {
+    if (threadIdx.x == 0) s_i = static_cast<int>(atomicAdd(ctr, 1u));
+    __syncthreads();
+    const int i = s_i;
+    if (i >= n_order) break;
     const int32_t u = order[i];
     const int64_t b = doff[u];
     const int n = static_cast<int>(doff[u + 1] - b);
-    const bool staged = n <= kCtaList;
+    const bool staged = n <= cap;
     const int32_t* list = staged ? s_big : dcol + b;
-    if (staged)
-      for (int k = threadIdx.x; k < n; k += kTcThreads) s_big[k] = dcol[b + k];
+    for (int k = threadIdx.x; k < kCtaFilterWords; k += kTcThreads) bits[k] = 0u;
     __syncthreads();
-    for (int k = wid; k < n; k += kTcWarps) cnt += tc_probe(doff, dcol, list, n, list[k], lane, 32, &work);
+    for (int k = threadIdx.x; k < n; k += kTcThreads) {
+      const int32_t x = dcol[b + k];
+      if (staged) s_big[k] = x;
+      const uint32_t h = tc_hash<kCtaFilterBits>(x);
+      atomicOr(&bits[h >> 5], 1u << (h & 31));
+    }
+    __syncthreads();
+    int qn = 0;
+    for (int k = wid; k < n; k += kTcWarps) {
+      const int32_t v = list[k];
+      const int64_t vb = doff[v];
+      tc_probe_filtered<kCtaFilterBits>(dcol, vb, static_cast<int>(doff[v + 1] - vb), list, n, bits, q, qn, lane,
+                                        cnt, work);
+    }
+    if (lane < qn) cnt += tc_search(list, n, q[lane]);
     __syncthreads();
   }
 #pragma unroll
@@ -221,7 +316,7 @@ extern "C" gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_sta
   GX_TRY(dev_alloc(&b.deg, static_cast<size_t>(V)));
   GX_TRY(dev_alloc(&b.cnt, static_cast<size_t>(V)));
   GX_TRY(dev_alloc(&b.out, 2));
-  GX_TRY(dev_alloc(&b.ctr, 1));
+  GX_TRY(dev_alloc(&b.ctr, 2));  // claim counters of the warp and CTA kernels
   const int grid = e->n_sm * 8;
   tc_degree_kernel<<<grid, 256, 0, s>>>(e->d_off, V, b.deg);
   tc_count_kernel<<<grid, 256, 0, s>>>(e->d_off, e->d_col, b.deg, V, b.cnt);
@@ -275,7 +370,7 @@ extern "C" gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_sta
     GX_CUDA(cudaMemcpyAsync(b.order, order.data(), sizeof(int32_t) * order.size(), cudaMemcpyHostToDevice, s));
   tc_fill_kernel<<<grid, 256, 0, s>>>(e->d_off, e->d_col, b.deg, V, b.doff, b.dcol);
   GX_CUDA(cudaMemsetAsync(b.out, 0, 2 * sizeof(unsigned long long), s));
-  GX_CUDA(cudaMemsetAsync(b.ctr, 0, sizeof(unsigned int), s));
+  GX_CUDA(cudaMemsetAsync(b.ctr, 0, 2 * sizeof(unsigned int), s));
   // The long lists run on the copy stream beside the warp kernel, so the
   // few CTAs they need do not hold the rest of the GPU idle.
   cudaEvent_t filled = nullptr, big_done = nullptr;
@@ -284,9 +379,16 @@ extern "C" gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_sta
     GX_CUDA(cudaEventCreateWithFlags(&big_done, cudaEventDisableTiming));
     GX_CUDA(cudaEventRecord(filled, s));
     GX_CUDA(cudaStreamWaitEvent(e->s_copy, filled, 0));
-    const size_t smem = sizeof(int32_t) * kCtaList;
+    // Shared memory for the longest list only (big[0]), so the CTAs leave
+    // room on their SMs for the warp kernel's.
+    const int cap = std::min(cnt[big[0]], kCtaList);
+    const size_t smem = sizeof(uint32_t) * (kCtaFilterWords + 64 * kTcWarps + static_cast<size_t>(cap));
     GX_CUDA(cudaFuncSetAttribute(tc_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
-    tc_cta_kernel<<<std::min(n_big, e->n_sm), kTcThreads, smem, e->s_copy>>>(b.doff, b.dcol, b.order, n_big, b.out);
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_cta_kernel, kTcThreads, smem);
+    const int grid_cta = std::min(n_big, std::max(1, per_sm) * e->n_sm);
+    tc_cta_kernel<<<grid_cta, kTcThreads, smem, e->s_copy>>>(b.doff, b.dcol, b.order, n_big, cap, b.ctr + 1,
+                                                             b.out);
     GX_CUDA(cudaEventRecord(big_done, e->s_copy));
   }
   if (n_small > 0) {
