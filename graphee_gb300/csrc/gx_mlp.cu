@@ -17,8 +17,10 @@
 // output approximates r where the L1 error lives.
 // Weights: FP32 master copy updated by Adam; every forward pass (training
 // and inference) uses the weights rounded to BF16, with FP32 accumulation.
-// Inference runs on the tensor cores (mma.sync m16n8k16 BF16, the layer-1
-// accumulators re-packed in registers as layer-2 A fragments); training runs
+// Inference runs on the tensor cores (mma.sync m16n8k16 in f16, in which the
+// BF16-rounded weights are exact; each layer's accumulators re-packed in
+// registers as the next layer's A fragments, GELUs on packed f16 pairs,
+// layer 3 as an MMA against the w3 column); training runs
 // hand-written FP32 forward/backward kernels whose per-CTA weight gradients
 // are summed in CTA order, so training is deterministic.
 #include <cuda_bf16.h>
@@ -48,7 +50,8 @@ constexpr int kPartStride = kNumParams + 3;  // gradient partial + loss
 constexpr float kLossWeightCap = 100.f;
 
 // GELU in its tanh form, 0.5 x (1 + tanh(sqrt(2/pi) (x + 0.044715 x^3))):
-// training uses tanhf, inference the hardware tanh.approx.f32.
+// training uses tanhf in FP32, inference the hardware tanh.approx.f16x2 on
+// packed pairs (gelu_h2).
 constexpr float kGeluC = 0.7978845608028654f;  // sqrt(2/pi)
 constexpr float kGeluA = 0.044715f;
 __device__ __forceinline__ float gelu(float x) {
@@ -57,14 +60,6 @@ __device__ __forceinline__ float gelu(float x) {
 __device__ __forceinline__ float gelu_grad(float x) {
   const float t = tanhf(kGeluC * (x + kGeluA * x * x * x));
   return 0.5f * (1.f + t) + 0.5f * x * (1.f - t * t) * kGeluC * (1.f + 3.f * kGeluA * x * x);
-}
-__device__ __forceinline__ float tanh_fast(float x) {
-  float y;
-  asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float gelu_fast(float x) {
-  return 0.5f * x * (1.f + tanh_fast(kGeluC * (x + kGeluA * x * x * x)));
 }
 __device__ __forceinline__ float softplus(float z) { return z > 20.f ? z : log1pf(expf(z)); }
 __device__ __forceinline__ float bf16r(float x) { return __bfloat162float(__float2bfloat16_rn(x)); }
@@ -255,41 +250,62 @@ __global__ void __launch_bounds__(256) mlp_heavy_features_kernel(const int64_t* 
   }
 }
 
-__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
-  const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+__device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
+  const __half2 h = __floats2half2_rn(lo, hi);
   return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+__device__ __forceinline__ void mma_f16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
   asm volatile(
-      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "mma.sync.aligned.m16n8k16.row.col.f32.f16.f16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
       "{%0,%1,%2,%3};\n"
       : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
 
-// Inference: 16 vertices per warp step on the tensor cores.  Writes s_v =
-// softplus(z_v) and each CTA's partial sums of s and of s over dangling
-// vertices.
+// GELU (tanh form) of two f16 values at once: 0.5 x + 0.5 x tanh(c x (1 +
+// a x^2)), written c x + (c a) x^3 inside.  Six packed instructions for two
+// values; for |x| > 255 the square overflows to inf and the result tends to
+// x or 0, the function's own limits.
+__device__ __forceinline__ uint32_t gelu_h2(uint32_t xr) {
+  const __half2 x = *reinterpret_cast<const __half2*>(&xr);
+  const __half2 c = __float2half2_rn(kGeluC), ca = __float2half2_rn(kGeluC * kGeluA), half = __float2half2_rn(0.5f);
+  const __half2 u = __hmul2(x, __hfma2(__hmul2(x, x), ca, c));
+  uint32_t ur = *reinterpret_cast<const uint32_t*>(&u), tr;
+  asm("tanh.approx.f16x2 %0, %1;" : "=r"(tr) : "r"(ur));
+  const __half2 hx = __hmul2(x, half);
+  const __half2 y = __hfma2(hx, *reinterpret_cast<const __half2*>(&tr), hx);
+  return *reinterpret_cast<const uint32_t*>(&y);
+}
+
+// Inference: 16 vertices per warp step on the tensor cores, all three layers
+// as f16 mma.sync m16n8k16 with FP32 accumulation.  The BF16-rounded weights
+// are exact in f16.  Each layer's accumulators plus bias are packed to f16x2
+// in registers, where they already sit as the next layer's A fragments; the
+// GELUs run on the packed pairs.  Layer 3 is an MMA against w3 as column 0
+// of an otherwise zero B, so lanes with t == 0 receive z of rows g and g+8.
+// Writes s_v = softplus(z_v) and each CTA's partial sums of s and of s over
+// dangling vertices.
 __global__ void __launch_bounds__(128) mlp_infer_kernel(const float* feat, const float* norm, const float* params,
                                                         int32_t V, float* s_out, double* part_sum,
                                                         double* part_dang) {
-  __shared__ __align__(16) __nv_bfloat16 sW1[kH][24];
-  __shared__ __align__(16) __nv_bfloat16 sW2[kH][72];
-  __shared__ float sb1[kH], sb2[kH], sw3[kH], sb3, smean[kF], sinv[kF];
+  __shared__ __align__(16) __half sW1[kH][24];
+  __shared__ __align__(16) __half sW2[kH][72];
+  __shared__ float sb1[kH], sb2[kH], sb3, smean[kF], sinv[kF];
+  __shared__ __align__(16) __half sw3[kH];
   __shared__ double s_red[2][4];
   for (int i = threadIdx.x; i < kH * 24; i += blockDim.x) {
     const int n = i / 24, k = i % 24;
-    sW1[n][k] = __float2bfloat16_rn(k < kF ? params[kOffW1 + n * kF + k] : 0.f);
+    sW1[n][k] = __float2half_rn(k < kF ? bf16r(params[kOffW1 + n * kF + k]) : 0.f);
   }
   for (int i = threadIdx.x; i < kH * 72; i += blockDim.x) {
     const int n = i / 72, k = i % 72;
-    sW2[n][k] = __float2bfloat16_rn(k < kH ? params[kOffW2 + n * kH + k] : 0.f);
+    sW2[n][k] = __float2half_rn(k < kH ? bf16r(params[kOffW2 + n * kH + k]) : 0.f);
   }
   for (int i = threadIdx.x; i < kH; i += blockDim.x) {
     sb1[i] = params[kOffB1 + i];
     sb2[i] = params[kOffB2 + i];
-    sw3[i] = bf16r(params[kOffW3 + i]);
+    sw3[i] = __float2half_rn(bf16r(params[kOffW3 + i]));
   }
   if (threadIdx.x == 0) sb3 = params[kOffB3];
   if (threadIdx.x < kF) {
@@ -300,6 +316,23 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const float* feat, const
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int g = lane >> 2, t = lane & 3;
   const int warps = gridDim.x * (blockDim.x >> 5);
+  // Per-lane constants: layer biases of this lane's output columns and the
+  // layer-3 B fragments (w3 in column 0: lanes with g == 0).
+  float bl1[8][2], bl2[8][2];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    bl1[j][0] = sb1[8 * j + 2 * t];
+    bl1[j][1] = sb1[8 * j + 2 * t + 1];
+    bl2[j][0] = sb2[8 * j + 2 * t];
+    bl2[j][1] = sb2[8 * j + 2 * t + 1];
+  }
+  uint32_t b3[4][2];
+#pragma unroll
+  for (int kk = 0; kk < 4; ++kk) {
+    b3[kk][0] = g == 0 ? *reinterpret_cast<const uint32_t*>(&sw3[16 * kk + 2 * t]) : 0u;
+    b3[kk][1] = g == 0 ? *reinterpret_cast<const uint32_t*>(&sw3[16 * kk + 8 + 2 * t]) : 0u;
+  }
+  const float b3s = sb3;
   double sum = 0, dang = 0;
   for (int grp = blockIdx.x * (blockDim.x >> 5) + wid; grp * 16 < V; grp += warps) {
     const int r0 = grp * 16 + g, r1 = r0 + 8;
@@ -315,29 +348,20 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const float* feat, const
         }
       }
     }
-    const uint32_t a1[4] = {pack_bf16(x[0][0], x[0][1]), pack_bf16(x[1][0], x[1][1]), 0u, 0u};
-    float h1[8][4];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      h1[j][0] = h1[j][1] = h1[j][2] = h1[j][3] = 0.f;
-      const uint32_t b0 = *reinterpret_cast<const uint32_t*>(&sW1[8 * j + g][2 * t]);
-      const uint32_t b1 = *reinterpret_cast<const uint32_t*>(&sW1[8 * j + g][2 * t + 8]);
-      mma_bf16(h1[j], a1, b0, b1);
-      const float bl = sb1[8 * j + 2 * t], bh = sb1[8 * j + 2 * t + 1];
-      h1[j][0] = gelu_fast(h1[j][0] + bl);
-      h1[j][1] = gelu_fast(h1[j][1] + bh);
-      h1[j][2] = gelu_fast(h1[j][2] + bl);
-      h1[j][3] = gelu_fast(h1[j][3] + bh);
-    }
+    const uint32_t a1[4] = {pack_h2(x[0][0], x[0][1]), pack_h2(x[1][0], x[1][1]), 0u, 0u};
+    // Layer 1 -> GELU -> layer-2 A fragments (k-step kk takes n-tiles 2kk, 2kk+1).
     uint32_t a2[4][4];
 #pragma unroll
-    for (int kk = 0; kk < 4; ++kk) {
-      a2[kk][0] = pack_bf16(h1[2 * kk][0], h1[2 * kk][1]);
-      a2[kk][1] = pack_bf16(h1[2 * kk][2], h1[2 * kk][3]);
-      a2[kk][2] = pack_bf16(h1[2 * kk + 1][0], h1[2 * kk + 1][1]);
-      a2[kk][3] = pack_bf16(h1[2 * kk + 1][2], h1[2 * kk + 1][3]);
+    for (int j = 0; j < 8; ++j) {
+      float h[4] = {0.f, 0.f, 0.f, 0.f};
+      const uint32_t b0 = *reinterpret_cast<const uint32_t*>(&sW1[8 * j + g][2 * t]);
+      const uint32_t b1 = *reinterpret_cast<const uint32_t*>(&sW1[8 * j + g][2 * t + 8]);
+      mma_f16(h, a1, b0, b1);
+      a2[j >> 1][(j & 1) * 2] = gelu_h2(pack_h2(h[0] + bl1[j][0], h[1] + bl1[j][1]));
+      a2[j >> 1][(j & 1) * 2 + 1] = gelu_h2(pack_h2(h[2] + bl1[j][0], h[3] + bl1[j][1]));
     }
-    float z0 = 0.f, z1 = 0.f;
+    // Layer 2 -> GELU -> layer-3 A fragments.
+    uint32_t a3[4][4];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       float c[4] = {0.f, 0.f, 0.f, 0.f};
@@ -345,22 +369,20 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const float* feat, const
       for (int kk = 0; kk < 4; ++kk) {
         const uint32_t b0 = *reinterpret_cast<const uint32_t*>(&sW2[8 * j + g][16 * kk + 2 * t]);
         const uint32_t b1 = *reinterpret_cast<const uint32_t*>(&sW2[8 * j + g][16 * kk + 8 + 2 * t]);
-        mma_bf16(c, a2[kk], b0, b1);
+        mma_f16(c, a2[kk], b0, b1);
       }
-      const int n0 = 8 * j + 2 * t;
-      z0 += gelu_fast(c[0] + sb2[n0]) * sw3[n0] + gelu_fast(c[1] + sb2[n0 + 1]) * sw3[n0 + 1];
-      z1 += gelu_fast(c[2] + sb2[n0]) * sw3[n0] + gelu_fast(c[3] + sb2[n0 + 1]) * sw3[n0 + 1];
+      a3[j >> 1][(j & 1) * 2] = gelu_h2(pack_h2(c[0] + bl2[j][0], c[1] + bl2[j][1]));
+      a3[j >> 1][(j & 1) * 2 + 1] = gelu_h2(pack_h2(c[2] + bl2[j][0], c[3] + bl2[j][1]));
     }
-    z0 += __shfl_xor_sync(0xffffffffu, z0, 1);
-    z0 += __shfl_xor_sync(0xffffffffu, z0, 2);
-    z1 += __shfl_xor_sync(0xffffffffu, z1, 1);
-    z1 += __shfl_xor_sync(0xffffffffu, z1, 2);
+    float z[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) mma_f16(z, a3[kk], b3[kk][0], b3[kk][1]);
     if (t == 0) {
 #pragma unroll
       for (int r = 0; r < 2; ++r) {
         const int v = r ? r1 : r0;
         if (v < V) {
-          const float sv = softplus((r ? z1 : z0) + sb3);
+          const float sv = softplus((r ? z[2] : z[0]) + b3s);
           s_out[v] = sv;
           sum += sv;
           if (feat[static_cast<size_t>(v) * kFeatStride + 5] != 0.f) dang += sv;
@@ -670,10 +692,13 @@ struct FeatScratch {
   double* part = nullptr;
   unsigned int* cursor = nullptr;
   int grid = 0;
+  cudaEvent_t ready = nullptr, heavy_done = nullptr;  // fork / join of the heavy lists' side stream
   ~FeatScratch() {
     dev_free(&nb);
     dev_free(&part);
     dev_free(&cursor);
+    if (ready) cudaEventDestroy(ready);
+    if (heavy_done) cudaEventDestroy(heavy_done);
   }
   gx_status alloc(const gx_engine* e) {
     int per_sm = 0;
@@ -682,6 +707,8 @@ struct FeatScratch {
     GX_TRY(dev_alloc(&nb, static_cast<size_t>(e->V)));
     GX_TRY(dev_alloc(&part, static_cast<size_t>(grid) + e->heavy.size()));
     GX_TRY(dev_alloc(&cursor, 1));
+    GX_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    GX_CUDA(cudaEventCreateWithFlags(&heavy_done, cudaEventDisableTiming));
     return GX_OK;
   }
 };
@@ -699,12 +726,21 @@ gx_status engine_features(gx_engine* e, double damping, float* feat, double* uni
   mlp_nbr_kernel<<<fs.grid, 256, 0, s>>>(e->d_off, e->d_outdeg, V, fs.nb);
   GX_CUDA(cudaMemsetAsync(fs.cursor, 0, sizeof(unsigned int), s));
   GX_CUDA(cudaMemsetAsync(fs.part, 0, sizeof(double) * fs.grid, s));
+  // The heavy lists (a CTA each) run on the engine's side stream beside the
+  // tile kernel; both write disjoint vertices' features and partials.  (With
+  // one CTA per SM instead, the hub lists became the critical path: 2.07 ->
+  // 2.63 ms at R-MAT scale 24.)
+  if (n_heavy) {
+    GX_CUDA(cudaEventRecord(fs.ready, s));
+    GX_CUDA(cudaStreamWaitEvent(e->s_copy, fs.ready, 0));
+    mlp_heavy_features_kernel<<<std::min(n_heavy, e->n_sm * 8), 256, 0, e->s_copy>>>(
+        e->d_off, e->d_col, e->d_outdeg, fs.nb, e->d_heavy, n_heavy, V, damping, dangling0, feat, fs.part + fs.grid);
+    GX_CUDA(cudaEventRecord(fs.heavy_done, e->s_copy));
+  }
   mlp_features_kernel<<<fs.grid, 256, 0, s>>>(e->d_off, e->d_col, e->d_outdeg, fs.nb, V, e->d_units,
                                                static_cast<int32_t>(e->units.size()), fs.cursor,
                                                n_heavy ? heavy_deg : INT64_MAX, damping, dangling0, feat, fs.part);
-  if (n_heavy)
-    mlp_heavy_features_kernel<<<std::min(n_heavy, e->n_sm * 8), 256, 0, s>>>(
-        e->d_off, e->d_col, e->d_outdeg, fs.nb, e->d_heavy, n_heavy, V, damping, dangling0, feat, fs.part + fs.grid);
+  if (n_heavy) GX_CUDA(cudaStreamWaitEvent(s, fs.heavy_done, 0));
   GX_CUDA(cudaGetLastError());
   std::vector<double> h(static_cast<size_t>(fs.grid) + n_heavy);
   GX_CUDA(cudaMemcpyAsync(h.data(), fs.part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, s));

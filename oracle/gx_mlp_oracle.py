@@ -46,6 +46,19 @@ def softplus(z):
     return np.where(z > 20, z, np.log1p(np.exp(np.minimum(z, 20))))
 
 
+def predict(params, norm, x_raw):
+    """softplus(z) of the network in FP64, with W1, W2, w3 rounded to BF16
+    as the library's forward passes use them (before normalisation to sum 1)."""
+    W1, b1, W2, b2, w3, b3 = unpack(params)
+    p32 = np.asarray(params, np.float32)
+    W1r = bf16_round(p32[:H * F]).reshape(H, F)
+    W2r = bf16_round(p32[H * F + H:H * F + H + H * H]).reshape(H, H)
+    w3r = bf16_round(p32[H * F + 2 * H + H * H:H * F + 3 * H + H * H])
+    norm = np.asarray(norm, np.float64)
+    X = (np.asarray(x_raw, np.float64) - norm[:F]) * norm[F:]
+    return softplus(gelu(gelu(X @ W1r.T + b1) @ W2r.T + b2) @ w3r + b3)
+
+
 def loss_and_grad(params, norm, x_raw, t):
     """Mean over samples of min(exp(t), 100) * (log softplus(z) - t)^2 and its gradient."""
     W1, b1, W2, b2, w3, b3 = unpack(params)

@@ -29,6 +29,30 @@ def test_gradient_matches_fp64_oracle():
     assert float(np.dot(g, ref_g)) > 0.99 * np.linalg.norm(g) * np.linalg.norm(ref_g)
 
 
+def test_inference_matches_fp64_forward():
+    """The tensor-core inference (f16 operands and activations, FP32
+    accumulation) against the FP64 forward pass of the same network on the
+    oracle's features, after normalisation to sum 1."""
+    g = gx.rmat_graph(14, 16, seed=11, P=4)
+    m = gx.MLP(seed=6)
+    p, _ = m.params()
+    rng = np.random.default_rng(2)
+    p = (p + rng.normal(0, 0.05, size=p.shape)).astype(np.float32)
+    F = MO.features(g.V, g.off, g.col, g.outdeg)
+    norm = np.concatenate([F.mean(0), 1.0 / (F.std(0) + 1e-6)]).astype(np.float32)
+    m.set_params(p, norm)
+    with gx.Engine() as e:
+        e.load(g)
+        pred, _ = m.predict(e)
+    ref = MO.predict(p, norm, F)
+    ref = ref / ref.sum()
+    pred = pred.astype(np.float64)
+    l1 = np.abs(pred - ref).sum()
+    rel = (np.abs(pred - ref) / ref).max()
+    print(f"inference vs FP64 forward: L1 {l1:.2e}, max relative {rel:.2e}")
+    assert l1 < 5e-3 and rel < 3e-2, (l1, rel)
+
+
 def test_prediction_is_normalised_and_training_reduces_loss():
     graphs = [gx.rmat_graph(s, 16, seed=100 + i, P=4) for i, s in enumerate([11, 12, 12, 13])]
     m = gx.MLP(seed=1)

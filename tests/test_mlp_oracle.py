@@ -108,3 +108,12 @@ def test_features_match_sparse_restatement():
     np.testing.assert_array_equal(f[:, 5], (np.asarray(g.outdeg) == 0).astype(np.float64))
     # the graph has every kind of vertex the features distinguish
     assert (indeg == 0).any() and (np.asarray(g.outdeg) == 0).any() and indeg.max() > 100
+
+
+def test_forward_is_the_loss_forward():
+    """predict() and the loss share one forward pass: targets equal to the
+    network's own log-outputs give zero loss and zero gradient."""
+    p, norm, x, _ = _problem(5)
+    t = np.log(MO.predict(p, norm, x))
+    loss, g = MO.loss_and_grad(p, norm, x, t)
+    assert loss < 1e-24 and np.abs(g).max() < 1e-12
