@@ -384,6 +384,26 @@ def run_gx(args, rank, local_rank, world):
                 "scanned_gteps": scanned / (ms_s / 1000) / 1e9, "ms_per_run": ms_s,
                 "supersteps": runs[-1]["iterations"], "push_supersteps": runs[-1]["push_iterations"],
                 "weights": "uint32 in [1,255], seeded", "source": 0}
+        # Per pull superstep: the pull kernel timed with CUDA events on the
+        # engine's stream (profiling engine), over the edges its pull steps
+        # scanned; algorithmic bytes 12 per edge (index, weight, distance
+        # gather) + 16 per vertex of the swept shards (offsets, old and new
+        # distance), the latter prorated by the edges a selective step swept.
+        pe = gx.Engine(device=local_rank, profile=1)
+        pe.load(g)
+        pe.set_weights(g.weights)
+        pe.run(gx.APP_SSSP, 10000, source=0, weighted=True)
+        pst = pe.run(gx.APP_SSSP, 10000, source=0, weighted=True)
+        steps = [pe.iter_stats(i) for i in range(pst["iterations"])]
+        pe.close()
+        pulled = [s for s in steps if s["mode"] in (0, 1)]
+        e_pull = sum(s["edges_scanned"] for s in pulled)
+        if pulled and pst["ms_pull"] > 0:
+            bytes_pull = 12 * e_pull + 16 * g.V * (e_pull / g.E)
+            ach = bytes_pull / (pst["ms_pull"] / 1000) / 1e9
+            sssp["pull_supersteps"] = {"count": len(pulled), "edges": e_pull, "ms_pull_kernels": pst["ms_pull"],
+                                       "gteps": e_pull / (pst["ms_pull"] / 1000) / 1e9, "achieved_gbs": ach,
+                                       "frac_of_measured_hbm": ach / measured_peak_hbm()[0]}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

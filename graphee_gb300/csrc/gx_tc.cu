@@ -46,17 +46,29 @@ __device__ __forceinline__ bool tc_before(int32_t du, int32_t u, int32_t dv, int
   return du < dv || (du == dv && u < v);
 }
 
-// |N+(u)| per vertex (self-loops never qualify: u is not before itself).
-__global__ void tc_count_kernel(const int64_t* off, const int32_t* col, const int32_t* deg, int32_t V,
-                                int32_t* cnt) {
+// Warp per vertex u.  Its list is read 8 chunks of 32 at a time, all ids
+// and their degrees loaded before any is used, so a hub's long list costs
+// one dependent load chain per 256 entries, not per 32 (the hubs set the
+// kernels' length).  Self-loops never qualify: u is not before itself.
+constexpr int kOrientChunks = 8;
+
+// |N+(u)| per vertex.
+__global__ void tc_count_kernel(const int64_t* __restrict__ off, const int32_t* __restrict__ col,
+                                const int32_t* __restrict__ deg, int32_t V, int32_t* __restrict__ cnt) {
   const int lane = threadIdx.x & 31;
   const int warps = gridDim.x * (blockDim.x >> 5);
   for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < V; u += warps) {
     const int32_t du = deg[u];
+    const int64_t e1 = off[u + 1];
     int c = 0;
-    for (int64_t k = off[u] + lane; k < off[u + 1]; k += 32) {
-      const int32_t v = col[k];
-      c += tc_before(du, u, deg[v], v);
+    for (int64_t base = off[u]; base < e1; base += 32 * kOrientChunks) {
+      int32_t v[kOrientChunks], dv[kOrientChunks];
+#pragma unroll
+      for (int j = 0; j < kOrientChunks; ++j) v[j] = base + 32 * j + lane < e1 ? col[base + 32 * j + lane] : 0;
+#pragma unroll
+      for (int j = 0; j < kOrientChunks; ++j) dv[j] = base + 32 * j + lane < e1 ? deg[v[j]] : 0;
+#pragma unroll
+      for (int j = 0; j < kOrientChunks; ++j) c += base + 32 * j + lane < e1 && tc_before(du, u, dv[j], v[j]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
@@ -64,25 +76,31 @@ __global__ void tc_count_kernel(const int64_t* off, const int32_t* col, const in
   }
 }
 
-// N+(u), in the input's ascending order, via ballot + popc compaction.
-__global__ void tc_fill_kernel(const int64_t* off, const int32_t* col, const int32_t* deg, int32_t V,
-                               const int64_t* doff, int32_t* dcol) {
+// N+(u), in the input's ascending order: chunk by chunk, ballot + popc
+// compaction.
+__global__ void tc_fill_kernel(const int64_t* __restrict__ off, const int32_t* __restrict__ col,
+                               const int32_t* __restrict__ deg, int32_t V, const int64_t* __restrict__ doff,
+                               int32_t* __restrict__ dcol) {
   const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
   const int warps = gridDim.x * (blockDim.x >> 5);
   for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < V; u += warps) {
     const int32_t du = deg[u];
     int64_t pos = doff[u];
-    for (int64_t base = off[u]; base < off[u + 1]; base += 32) {
-      const int64_t k = base + lane;
-      int32_t v = 0;
-      bool keep = false;
-      if (k < off[u + 1]) {
-        v = col[k];
-        keep = tc_before(du, u, deg[v], v);
+    const int64_t e1 = off[u + 1];
+    for (int64_t base = off[u]; base < e1; base += 32 * kOrientChunks) {
+      int32_t v[kOrientChunks], dv[kOrientChunks];
+#pragma unroll
+      for (int j = 0; j < kOrientChunks; ++j) v[j] = base + 32 * j + lane < e1 ? col[base + 32 * j + lane] : 0;
+#pragma unroll
+      for (int j = 0; j < kOrientChunks; ++j) dv[j] = base + 32 * j + lane < e1 ? deg[v[j]] : 0;
+#pragma unroll
+      for (int j = 0; j < kOrientChunks; ++j) {
+        const bool keep = base + 32 * j + lane < e1 && tc_before(du, u, dv[j], v[j]);
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) dcol[pos + __popc(m & below)] = v[j];
+        pos += __popc(m);
       }
-      const unsigned m = __ballot_sync(0xffffffffu, keep);
-      if (keep) dcol[pos + __popc(m & ((1u << lane) - 1u))] = v;
-      pos += __popc(m);
     }
   }
 }
