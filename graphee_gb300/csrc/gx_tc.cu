@@ -131,10 +131,12 @@ __device__ __forceinline__ uint32_t tc_hash(int32_t w) {
 // filter.  Most probes miss (about 90% on R-MAT) and the filter rejects all
 // but 1-2% of those with one shared-memory load; the ids that pass are
 // appended to the warp's queue (ballot + prefix) and binary-searched 32 at a
-// time, so the searches run with every lane busy.  qn (warp-uniform) is the
-// queue's fill, below 32 between calls.  N+(v) lies at dcol[vb, vb + len);
-// each round's id is loaded one round ahead, so the load's latency overlaps
-// the current round's filter test.
+// time, so the searches run with every lane busy.  Two rounds of 32 ids go
+// through per loop step, each round's ids loaded a step ahead so the loads'
+// latency overlaps the filter tests.  qn (warp-uniform) is the queue's fill:
+// below 32 between steps, at most 95 after a step's appends (kQueue slots).
+// N+(v) lies at dcol[vb, vb + len).
+constexpr int kQueue = 96;
 template <int BITS>
 __device__ __forceinline__ void tc_probe_filtered(const int32_t* __restrict__ dcol, int64_t vb, int len,
                                                   const int32_t* list, int n, const uint32_t* bits, int32_t* q,
@@ -143,24 +145,31 @@ __device__ __forceinline__ void tc_probe_filtered(const int32_t* __restrict__ dc
   const int32_t* nv = dcol + vb;
   if (lane == 0) work += static_cast<unsigned long long>(len);
   const unsigned below = (1u << lane) - 1u;
-  int32_t w_next = lane < len ? nv[lane] : 0;
-  for (int base = 0; base < len; base += 32) {
-    const int j = base + lane;
-    const int32_t w = w_next;
-    if (j + 32 < len) w_next = nv[j + 32];
-    bool pass = false;
-    if (j < len) {
-      const uint32_t h = tc_hash<BITS>(w);
-      pass = (bits[h >> 5] >> (h & 31)) & 1u;
+  int32_t n0 = lane < len ? nv[lane] : 0, n1 = lane + 32 < len ? nv[lane + 32] : 0;
+  for (int base = 0; base < len; base += 64) {
+    const int j0 = base + lane, j1 = j0 + 32;
+    const int32_t w0 = n0, w1 = n1;
+    if (j0 + 64 < len) n0 = nv[j0 + 64];
+    if (j1 + 64 < len) n1 = nv[j1 + 64];
+    bool p0 = false, p1 = false;
+    if (j0 < len) {
+      const uint32_t h = tc_hash<BITS>(w0);
+      p0 = (bits[h >> 5] >> (h & 31)) & 1u;
     }
-    const unsigned m = __ballot_sync(0xffffffffu, pass);
-    if (pass) q[qn + __popc(m & below)] = w;
-    qn += __popc(m);
-    if (qn >= 32) {
+    if (j1 < len) {
+      const uint32_t h = tc_hash<BITS>(w1);
+      p1 = (bits[h >> 5] >> (h & 31)) & 1u;
+    }
+    const unsigned m0 = __ballot_sync(0xffffffffu, p0), m1 = __ballot_sync(0xffffffffu, p1);
+    if (p0) q[qn + __popc(m0 & below)] = w0;
+    qn += __popc(m0);
+    if (p1) q[qn + __popc(m1 & below)] = w1;
+    qn += __popc(m1);
+    while (qn >= 32) {
       __syncwarp();
       cnt += tc_search(list, n, q[lane]);
       __syncwarp();
-      if (lane < qn - 32) q[lane] = q[32 + lane];
+      for (int i = lane; i < qn - 32; i += 32) q[i] = q[32 + i];
       qn -= 32;
     }
   }
@@ -173,7 +182,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_warp_kernel(const int64_t* doff
                                                              unsigned long long* out) {
   __shared__ int32_t s_list[kTcWarps][kWarpList];
   __shared__ uint32_t s_bits[kTcWarps][kFilterWords];
-  __shared__ int32_t s_q[kTcWarps][64];
+  __shared__ int32_t s_q[kTcWarps][kQueue];
   __shared__ unsigned long long s_red[2][kTcWarps];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   int32_t* list = s_list[wid];
@@ -245,8 +254,8 @@ __global__ void __launch_bounds__(kTcThreads) tc_cta_kernel(const int64_t* doff,
                                                             unsigned int* ctr, unsigned long long* out) {
   extern __shared__ uint32_t s_dyn[];
   uint32_t* bits = s_dyn;
-  int32_t* q = reinterpret_cast<int32_t*>(s_dyn + kCtaFilterWords) + 64 * (threadIdx.x >> 5);
-  int32_t* s_big = reinterpret_cast<int32_t*>(s_dyn + kCtaFilterWords) + 64 * kTcWarps;
+  int32_t* q = reinterpret_cast<int32_t*>(s_dyn + kCtaFilterWords) + kQueue * (threadIdx.x >> 5);
+  int32_t* s_big = reinterpret_cast<int32_t*>(s_dyn + kCtaFilterWords) + kQueue * kTcWarps;
   __shared__ unsigned long long s_red[2][kTcWarps];
   __shared__ int s_i;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -400,7 +409,7 @@ extern "C" gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_sta
     // Shared memory for the longest list only (big[0]), so the CTAs leave
     // room on their SMs for the warp kernel's.
     const int cap = std::min(cnt[big[0]], kCtaList);
-    const size_t smem = sizeof(uint32_t) * (kCtaFilterWords + 64 * kTcWarps + static_cast<size_t>(cap));
+    const size_t smem = sizeof(uint32_t) * (kCtaFilterWords + kQueue * kTcWarps + static_cast<size_t>(cap));
     GX_CUDA(cudaFuncSetAttribute(tc_cta_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tc_cta_kernel, kTcThreads, smem);
