@@ -287,7 +287,7 @@ extern "C" int gxo_run(int app, int32_t V, int32_t P, const int32_t* bounds, con
 
   if (app == GXO_INDEGREE) {
     std::vector<int32_t> Msg(V, 0);  // cal.cpp:77
-    auto comp = [&](int32_t p, int32_t* M, int32_t* MN, int32_t* Val) -> int64_t {
+    auto comp = [&](int32_t p, int32_t* /*Msg: unused, the in-degree reads no values*/, int32_t* MN, int32_t* Val) -> int64_t {
       int64_t ch = 0;
       for (int32_t v = bounds[p]; v < bounds[p + 1]; ++v) {
         int32_t rel = static_cast<int32_t>(off[v + 1] - off[v]);  // cal.cpp:43
