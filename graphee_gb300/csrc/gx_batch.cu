@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "gx_engine.h"
+#include "gx_nvtx.h"
 
 using namespace gx;
 
@@ -476,6 +477,7 @@ void gx_batch_tuning_default(gx_batch_tuning* t) {
 gx_status gx_batch_run(gx_engine* e, int32_t n_inst, const int32_t* inst_vbegin, int32_t pr_iters, int32_t cc_max_iter,
                        double damping, const gx_batch_tuning* tuning, float* pr_out, int32_t* cc_out,
                        int32_t* pr_steps, int32_t* cc_steps, gx_run_stats* stats) {
+  gx::NvtxRange nvtx_range("gx_batch_run");
   if (!e || n_inst < 1 || !inst_vbegin || pr_iters < 0 || cc_max_iter < 0)
     return fail(GX_ERR_INVALID, "gx_batch_run: bad arguments");
   if (!e->loaded || !e->all_resident) return fail(GX_ERR_STATE, "gx_batch_run: load the packed graph first (all resident)");
@@ -517,6 +519,7 @@ gx_status gx_batch_run(gx_engine* e, int32_t n_inst, const int32_t* inst_vbegin,
 
 gx_status gx_batch_autotune(gx_engine* e, int32_t n_inst, const int32_t* inst_vbegin, int32_t pr_iters,
                             int32_t cc_max_iter, const char* table_path, gx_batch_tuning* best, double* best_ms) {
+  gx::NvtxRange nvtx_range("gx_batch_autotune");
   if (!e || !best || n_inst < 1 || !inst_vbegin) return fail(GX_ERR_INVALID, "gx_batch_autotune: bad arguments");
   if (!e->loaded || !e->all_resident) return fail(GX_ERR_STATE, "gx_batch_autotune: load the packed graph first");
   GX_CUDA(cudaSetDevice(e->dev));

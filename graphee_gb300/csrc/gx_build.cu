@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "gx_engine.h"
+#include "gx_nvtx.h"
 
 using namespace gx;
 
@@ -417,6 +418,7 @@ extern "C" {
 
 gx_status gx_build_csc_gpu(int32_t device, int32_t V, int64_t n, const int32_t* src, const int32_t* dst,
                            int32_t flags, int64_t* off, int32_t* col, int64_t* n_out) {
+  gx::NvtxRange nvtx_range("gx_build_csc_gpu");
   if (V < 0 || n < 0 || !off || (n > 0 && (!src || !dst || !col)) || !n_out)
     return fail(GX_ERR_INVALID, "gx_build_csc_gpu: bad arguments");
   BuildBuffers B;
@@ -450,6 +452,7 @@ gx_status gx_build_csc_gpu(int32_t device, int32_t V, int64_t n, const int32_t* 
 
 gx_status gx_rmat_csc_gpu(int32_t device, int32_t scale, int64_t n, double a, double b, double c, uint64_t seed,
                           int32_t flags, int64_t* off, int32_t* col, int64_t* n_out) {
+  gx::NvtxRange nvtx_range("gx_rmat_csc_gpu");
   if (scale < 1 || scale > 30 || n < 0 || !off || (n > 0 && !col) || !n_out)
     return fail(GX_ERR_INVALID, "gx_rmat_csc_gpu: bad arguments (scale %d, n %lld)", scale,
                 static_cast<long long>(n));

@@ -30,6 +30,7 @@
 #include <vector>
 
 #include "gx_engine.h"
+#include "gx_nvtx.h"
 
 #include <mutex>
 
@@ -1183,6 +1184,7 @@ gx_status gx_release_cached_memory(int32_t device) {
 
 gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds, const int64_t* off,
                       const int32_t* col, const int32_t* outdeg) {
+  gx::NvtxRange nvtx_range("gx_load_csc");
   const auto t_start = std::chrono::steady_clock::now();
   auto phase = [&](const char* what) {
     if (e && e->cfg.verbose)
@@ -1363,6 +1365,7 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
 }
 
 gx_status gx_load_shards(gx_engine* e, const char* dir, int32_t V, int32_t P) {
+  gx::NvtxRange nvtx_range("gx_load_shards");
   if (!e || !dir) return fail(GX_ERR_INVALID, "gx_load_shards: bad arguments");
   int64_t E = 0;
   GX_TRY(gx_read_shards(dir, V, P, nullptr, nullptr, nullptr, nullptr, &E));
@@ -1374,6 +1377,7 @@ gx_status gx_load_shards(gx_engine* e, const char* dir, int32_t V, int32_t P) {
 }
 
 gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
+  gx::NvtxRange nvtx_range("gx_set_weights");
   if (!e || !w) return fail(GX_ERR_INVALID, "gx_set_weights: bad arguments");
   if (!e->loaded) return fail(GX_ERR_STATE, "gx_set_weights: no graph loaded");
   GX_CUDA(cudaSetDevice(e->dev));
@@ -1452,6 +1456,7 @@ gx_status gx_set_init(gx_engine* e, const void* host_vals) {
 }
 
 gx_status gx_run(gx_engine* e, const gx_run_params* prm, gx_run_stats* stats) {
+  gx::NvtxRange nvtx_range("gx_run");
   if (!e || !prm) return fail(GX_ERR_INVALID, "gx_run: bad arguments");
   if (!e->loaded) return fail(GX_ERR_STATE, "gx_run: no graph loaded");
   if (prm->max_iter < 0) return fail(GX_ERR_INVALID, "gx_run: max_iter < 0");
@@ -1490,6 +1495,7 @@ gx_status gx_run(gx_engine* e, const gx_run_params* prm, gx_run_stats* stats) {
 }
 
 gx_status gx_get_values(gx_engine* e, void* host_out) {
+  gx::NvtxRange nvtx_range("gx_get_values");
   if (!e || !host_out) return fail(GX_ERR_INVALID, "gx_get_values: bad arguments");
   if (!e->loaded) return fail(GX_ERR_STATE, "gx_get_values: no graph loaded");
   GX_CUDA(cudaSetDevice(e->dev));

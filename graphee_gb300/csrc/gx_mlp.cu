@@ -34,6 +34,7 @@
 #include <vector>
 
 #include "gx_engine.h"
+#include "gx_nvtx.h"
 
 using namespace gx;
 
@@ -829,6 +830,7 @@ gx_status gx_mlp_set_params(gx_mlp* m, const float* params, const float* norm) {
 }
 
 gx_status gx_mlp_add_graph(gx_mlp* m, gx_engine* e, int32_t max_samples, int32_t max_iter, double tolerance) {
+  gx::NvtxRange nvtx_range("gx_mlp_add_graph");
   if (!m || !e || max_samples < 1) return fail(GX_ERR_INVALID, "gx_mlp_add_graph: bad arguments");
   if (!e->loaded || !e->all_resident) return fail(GX_ERR_STATE, "gx_mlp_add_graph: load a resident graph first");
   if (e->dev != m->dev) return fail(GX_ERR_INVALID, "gx_mlp_add_graph: engine and MLP on different devices");
@@ -874,6 +876,7 @@ gx_status gx_mlp_add_graph(gx_mlp* m, gx_engine* e, int32_t max_samples, int32_t
 }
 
 gx_status gx_mlp_train(gx_mlp* m, int32_t epochs, int32_t batch, double lr, double* final_loss) {
+  gx::NvtxRange nvtx_range("gx_mlp_train");
   if (!m || epochs < 0 || batch < kTrainSamples) return fail(GX_ERR_INVALID, "gx_mlp_train: bad arguments");
   if (m->n == 0) return fail(GX_ERR_STATE, "gx_mlp_train: no training samples (gx_mlp_add_graph)");
   GX_CUDA(cudaSetDevice(m->dev));
@@ -950,6 +953,7 @@ gx_status gx_mlp_grad(gx_mlp* m, const float* host_x, const float* host_t, int32
 
 gx_status gx_mlp_predict(gx_mlp* m, gx_engine* e, double damping, float* host_out, double* ms_features,
                          double* ms_mlp) {
+  gx::NvtxRange nvtx_range("gx_mlp_predict");
   if (!m || !e) return fail(GX_ERR_INVALID, "gx_mlp_predict: bad arguments");
   if (!e->loaded || !e->all_resident) return fail(GX_ERR_STATE, "gx_mlp_predict: load a resident graph first");
   GX_CUDA(cudaSetDevice(e->dev));
@@ -1002,6 +1006,7 @@ gx_status gx_mlp_predict(gx_mlp* m, gx_engine* e, double damping, float* host_ou
 
 gx_status gx_pagerank_warm(gx_engine* e, gx_mlp* m, int32_t max_iter, double tolerance, double damping,
                            gx_warm_stats* out) {
+  gx::NvtxRange nvtx_range("gx_pagerank_warm");
   if (!e || !m || max_iter < 1) return fail(GX_ERR_INVALID, "gx_pagerank_warm: bad arguments");
   const auto t0 = std::chrono::steady_clock::now();
   gx_warm_stats ws{};

@@ -17,6 +17,7 @@
 #include <vector>
 
 #include "gx_engine.h"
+#include "gx_nvtx.h"
 
 using namespace gx;
 
@@ -141,6 +142,7 @@ __global__ void ppr_init_kernel(float* rs, const int32_t* outdeg, const int32_t*
 
 extern "C" gx_status gx_ppr(gx_engine* e, int32_t k, const int32_t* sources, int32_t iters, double restart,
                             float* host_out, gx_run_stats* stats) {
+  gx::NvtxRange nvtx_range("gx_ppr");
   if (!e || !sources || k < 1 || k > kPprCols || iters < 0 || restart < 0 || restart > 1)
     return fail(GX_ERR_INVALID, "gx_ppr: bad arguments (k must be 1..64)");
   if (!e->loaded) return fail(GX_ERR_STATE, "gx_ppr: no graph loaded");

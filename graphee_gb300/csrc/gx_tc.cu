@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "gx_engine.h"
+#include "gx_nvtx.h"
 
 using namespace gx;
 
@@ -328,6 +329,7 @@ struct TcBuffers {
 }  // namespace
 
 extern "C" gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_stats* stats) {
+  gx::NvtxRange nvtx_range("gx_triangle_count");
   if (!e || !total) return fail(GX_ERR_INVALID, "gx_triangle_count: bad arguments");
   if (!e->loaded) return fail(GX_ERR_STATE, "gx_triangle_count: no graph loaded");
   if (!e->all_resident)
