@@ -22,6 +22,8 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cstring>
+#include <memory>
 #include <numeric>
 #include <vector>
 
@@ -351,13 +353,15 @@ extern "C" gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_sta
   tc_count_kernel<<<grid, 256, 0, s>>>(e->d_off, e->d_col, b.deg, V, b.cnt);
   GX_CUDA(cudaGetLastError());
   // Offsets of N+ and the claim order (descending |N+|, by power-of-two bins).
-  std::vector<int32_t> cnt(V);
-  GX_CUDA(cudaMemcpyAsync(cnt.data(), b.cnt, sizeof(int32_t) * V, cudaMemcpyDeviceToHost, s));
+  // Host buffers are not zero-filled (every element is written below) and are
+  // first touched by the threads that fill them.
+  std::unique_ptr<int32_t[]> cnt(new int32_t[V]);
+  GX_CUDA(cudaMemcpyAsync(cnt.get(), b.cnt, sizeof(int32_t) * V, cudaMemcpyDeviceToHost, s));
   GX_CUDA(cudaStreamSynchronize(s));
   // Prefix sums and the claim order on the host threads: each thread scans
   // and bins a contiguous block of vertices; blocks are joined in order.
   const int nt = std::max(1, omp_get_max_threads());
-  std::vector<int64_t> doff(static_cast<size_t>(V) + 1, 0);
+  std::unique_ptr<int64_t[]> doff(new int64_t[static_cast<size_t>(V) + 1]);
   std::vector<int64_t> part(static_cast<size_t>(nt) + 1, 0);
   std::vector<std::vector<std::vector<int32_t>>> tbins(nt, std::vector<std::vector<int32_t>>(34));
 #pragma omp parallel num_threads(nt)
@@ -383,20 +387,35 @@ extern "C" gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_sta
   }
   doff[V] = part[nt];
   const int64_t m = doff[V];
+  // Claim order: the long lists sorted by (|N+| descending, id), then bins 32
+  // down to 0, each bin in thread order; copied in parallel to offsets
+  // computed first.
   std::vector<int32_t> big;
   for (int t = 0; t < nt; ++t) big.insert(big.end(), tbins[t][33].begin(), tbins[t][33].end());
   std::sort(big.begin(), big.end(), [&](int32_t a, int32_t c) { return cnt[a] > cnt[c] || (cnt[a] == cnt[c] && a < c); });
-  std::vector<int32_t> order(big);
-  for (int k = 32; k >= 0; --k)
-    for (int t = 0; t < nt; ++t) order.insert(order.end(), tbins[t][k].begin(), tbins[t][k].end());
   const int32_t n_big = static_cast<int32_t>(big.size());
-  const int32_t n_small = static_cast<int32_t>(order.size()) - n_big;
+  std::vector<int64_t> at(static_cast<size_t>(33) * nt);
+  int64_t n_order = n_big;
+  for (int k = 32; k >= 0; --k)
+    for (int t = 0; t < nt; ++t) {
+      at[static_cast<size_t>(k) * nt + t] = n_order;
+      n_order += static_cast<int64_t>(tbins[t][k].size());
+    }
+  std::unique_ptr<int32_t[]> order(new int32_t[std::max<int64_t>(n_order, 1)]);
+  if (n_big) memcpy(order.get(), big.data(), sizeof(int32_t) * n_big);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nt)
+  for (int i = 0; i < 33 * nt; ++i) {
+    const int k = i / nt, t = i % nt;
+    const std::vector<int32_t>& bin = tbins[t][k];
+    if (!bin.empty()) memcpy(order.get() + at[i], bin.data(), sizeof(int32_t) * bin.size());
+  }
+  const int32_t n_small = static_cast<int32_t>(n_order) - n_big;
   GX_TRY(dev_alloc(&b.doff, static_cast<size_t>(V) + 1));
   GX_TRY(dev_alloc(&b.dcol, static_cast<size_t>(m) + 1));
-  GX_TRY(dev_alloc(&b.order, order.size() + 1));
-  GX_CUDA(cudaMemcpyAsync(b.doff, doff.data(), sizeof(int64_t) * (V + 1), cudaMemcpyHostToDevice, s));
-  if (!order.empty())
-    GX_CUDA(cudaMemcpyAsync(b.order, order.data(), sizeof(int32_t) * order.size(), cudaMemcpyHostToDevice, s));
+  GX_TRY(dev_alloc(&b.order, static_cast<size_t>(n_order) + 1));
+  GX_CUDA(cudaMemcpyAsync(b.doff, doff.get(), sizeof(int64_t) * (V + 1), cudaMemcpyHostToDevice, s));
+  if (n_order > 0)
+    GX_CUDA(cudaMemcpyAsync(b.order, order.get(), sizeof(int32_t) * n_order, cudaMemcpyHostToDevice, s));
   tc_fill_kernel<<<grid, 256, 0, s>>>(e->d_off, e->d_col, b.deg, V, b.doff, b.dcol);
   GX_CUDA(cudaMemsetAsync(b.out, 0, 2 * sizeof(unsigned long long), s));
   GX_CUDA(cudaMemsetAsync(b.ctr, 0, 2 * sizeof(unsigned int), s));
