@@ -246,12 +246,12 @@ __global__ void __launch_bounds__(kTcThreads) tc_warp_kernel(const int64_t* doff
   }
 }
 
-// CTA per vertex for |N+(u)| > kWarpList: the list is staged in dynamic
-// shared memory when it fits, else searched where it lies.
-// Dynamic shared memory: the 2^16-bit filter, the warps' queues, then room
-// for `cap` list entries (the longest list of the launch, at most kCtaList).
-// Vertices are claimed one at a time from ctr; warps split N+(u) and probe
-// through the filter like the warp kernel.
+// CTA per vertex for |N+(u)| > kWarpList, claimed one at a time from ctr;
+// the CTA's warps split N+(u) and probe through the filter like the warp
+// kernel.  Dynamic shared memory holds the 2^16-bit filter, the warps'
+// queues, then room for `cap` list entries (the longest list of the launch,
+// at most kCtaList); a longer list is searched where it lies in global
+// memory, its filter still in shared memory.
 __global__ void __launch_bounds__(kTcThreads) tc_cta_kernel(const int64_t* doff, const int32_t* dcol,
                                                             const int32_t* order, int32_t n_order, int cap,
                                                             unsigned int* ctr, unsigned long long* out) {
