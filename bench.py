@@ -1,14 +1,15 @@
 #!/usr/bin/env python
 """PageRank GTEPS of GraphMP's shard-wise gather-apply on one GB300.
 
-Workload (default): seeded R-MAT, scale 24, edge factor 16 (a,b,c,d =
+Workload (default): seeded R-MAT, scale 26, edge factor 16 (a,b,c,d =
 .57/.19/.19/.05, self-loops and duplicates removed), 256 edge-balanced
 destination-range shards; one step = one PageRank run of 20 supersteps with
 the reference's semantics (comp_pagerank<float>, GraphMP/app/pagerank.cpp).
 value = 20 * E / step time, in GTEPS, inputs resident in HBM; e2e = the same
 metric through the C ABI with host buffers: one engine, and per step a load
 of the graph from the caller's arrays, the run, and the read-back of the
-ranks into the caller's buffer.
+ranks into the caller's buffer.  The line also carries weighted SSSP on the
+same graph and the scale-24 PageRank figures.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gx|reference]
 
@@ -17,7 +18,8 @@ Under torchrun (N > 1) every rank runs an independent replica on its own GPU
 `--impl reference` times the reference's CPU PageRank on this host's cores
 instead: its own app, compiled from the reference sources, where that binary
 was built for this host, else the oracle's restatement of GraphMP's OpenMP
-engine.
+engine.  That arm builds its graph with the oracle's restatement of the
+generator and never loads this package's library.
 """
 from __future__ import annotations
 
@@ -61,13 +63,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gx", choices=["gx", "reference"])
-    ap.add_argument("--scale", type=int, default=24)
+    ap.add_argument("--scale", type=int, default=26)
     ap.add_argument("--edge-factor", type=int, default=16)
     ap.add_argument("--iters", type=int, default=20)
     ap.add_argument("--cpu-iters", type=int, default=2, help="PageRank supersteps in the CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-sssp", action="store_true", help="skip the SSSP keys of the default run")
+    ap.add_argument("--no-scale24", action="store_true", help="skip the scale-24 keys of the default run")
     ap.add_argument("--workload", default="pagerank",
                     choices=["pagerank", "cc_tc", "stream", "batch", "ppr", "warm"],
                     help="pagerank = the headline run; the others measure the remaining configurations")
@@ -209,11 +212,11 @@ def _reference_pagerank(g, iters):
     import re
     if not (REF_BIN.exists() and os.access(REF_BIN, os.X_OK)):
         return None
-    import graphee_gb300 as gx
+    O = _oracle()
     key = id(g)
     if key not in _ref_dirs:
         d = tempfile.TemporaryDirectory(prefix="gx_ref_shards_")
-        gx.write_shards(g, d.name + "/")
+        O.write_shards(g, d.name + "/")
         _ref_dirs[key] = d
     d = _ref_dirs[key].name + "/"
     threads = min(os.cpu_count() or 1, REF_CMPNUM)
@@ -228,9 +231,16 @@ def _reference_pagerank(g, iters):
     if r.returncode != 0:
         return None
     ms = [int(m) for m in re.findall(r"Iteration: \d+, uses (\d+) ms", r.stderr)]
-    if len(ms) != iters + 1:
+    # Whole milliseconds: a graph whose supersteps round to 0 ms is timed by the port.
+    if len(ms) != iters + 1 or sum(ms[1:]) == 0:
         return None
     return sum(ms[1:]) / 1000.0, wall, threads, "reference"
+
+
+def _oracle():
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import gx_oracle as O
+    return O
 
 
 CPU_SAMPLE = {"reference": "the reference's own PageRank app (in-RAM edge cache on; "
@@ -246,8 +256,7 @@ def cpu_pagerank(g, iters):
     got = _reference_pagerank(g, iters)
     if got is not None:
         return got
-    sys.path.insert(0, str(ROOT / "oracle"))
-    import gx_oracle as O
+    O = _oracle()
     threads = os.cpu_count() or 1
     t0 = time.perf_counter()
     _, _, ms = O.run(O.PAGERANK_REF, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, iters, threads=threads)
@@ -259,17 +268,22 @@ def workload_name(args):
     return f"rmat{args.scale}"
 
 
-def base_config(args, g):
+def base_config(args, g, world):
+    """The workload, the same dict in both arms."""
     return {"workload": f"R-MAT scale {args.scale} edge factor {args.edge_factor} (a,b,c=.57,.19,.19), "
                         f"{args.iters} PageRank supersteps (reference semantics), {SHARDS} shards",
             "vertices": g.V, "edges": g.E, "shards": SHARDS, "supersteps": args.iters, "seed": SEED,
-            "l2": "inputs larger than L2 (column indices 4E bytes); no flush"}
+            "l2": "inputs larger than L2 (column indices 4E bytes); no flush",
+            "parallelism": f"replicas{world}"}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return 0
-    g, build_s = build_graph(args)
+    O = _oracle()
+    t0 = time.time()
+    g = O.rmat_graph(args.scale, args.edge_factor, seed=SEED, P=SHARDS)
+    build_s = time.time() - t0
     for _ in range(args.warmup):
         cpu_pagerank(g, args.cpu_iters)
     secs = []
@@ -282,13 +296,24 @@ def run_reference(args, rank, world):
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total / args.steps * 1000, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded R-MAT)",
-            "config": base_config(args, g),
+            "config": base_config(args, g, world),
+            "graph_build": {"s": round(build_s, 1), "by": "the oracle's restatement of the generator, on the host"},
             "cpu_baseline": {"value": value, "unit": "GTEPS", "cores": threads, "kind": kind,
                              "sample": f"{args.cpu_iters} of {args.iters} supersteps per step, same graph; "
                                        f"{CPU_SAMPLE[kind]}"},
             "e2e": {"value": value, "unit": "GTEPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def pull_kernel_ms(gx, g, device, iters):
+    """Average pull-kernel launch time of a PageRank run (CUDA events on the
+    engine's stream, one engine with per-launch timing)."""
+    with gx.Engine(device=device, profile=1) as prof:
+        prof.load(g)
+        prof.run(gx.APP_PAGERANK_REF, iters)
+        ps = prof.run(gx.APP_PAGERANK_REF, iters)
+    return ps["ms_pull"] / max(ps["pull_launches"], 1)
 
 
 def run_gx(args, rank, local_rank, world):
@@ -333,12 +358,7 @@ def run_gx(args, rank, local_rank, world):
     value = eps / 1e9
 
     # Dominant kernel, timed live with CUDA events on the engine's stream.
-    prof = gx.Engine(device=local_rank, profile=1)
-    prof.load(g)
-    prof.run(gx.APP_PAGERANK_REF, args.iters)
-    ps = prof.run(gx.APP_PAGERANK_REF, args.iters)
-    prof.close()
-    pull_ms = ps["ms_pull"] / max(ps["pull_launches"], 1)
+    pull_ms = pull_kernel_ms(gx, g, local_rank, args.iters)
     alg_bytes = 8 * g.E + 24 * g.V
     peak, peak_kind = measured_peak_hbm()
     achieved = alg_bytes / (pull_ms / 1000) / 1e9
@@ -405,6 +425,25 @@ def run_gx(args, rank, local_rank, world):
                                        "gteps": e_pull / (pst["ms_pull"] / 1000) / 1e9, "achieved_gbs": ach,
                                        "frac_of_measured_hbm": ach / measured_peak_hbm()[0]}
 
+    # The scale-24 graph of the earlier headline: PageRank GTEPS and the pull
+    # kernel's fraction of measured HBM bandwidth.
+    rmat24 = None
+    if args.scale == 26 and not args.no_scale24:
+        g24 = gx.rmat_graph(24, args.edge_factor, seed=SEED, P=SHARDS, gpu=True, device=local_rank)
+        with gx.Engine(device=local_rank) as e24:
+            e24.load(g24)
+            for _ in range(args.warmup):
+                e24.run(gx.APP_PAGERANK_REF, args.iters)
+            runs24 = [e24.run(gx.APP_PAGERANK_REF, args.iters) for _ in range(args.steps)]
+        launches += sum(r["kernel_launches"] for r in runs24)
+        ms24 = sum(r["ms_total"] for r in runs24) / len(runs24)
+        k24 = pull_kernel_ms(gx, g24, local_rank, args.iters)
+        b24 = 8 * g24.E + 24 * g24.V
+        rmat24 = {"value": g24.E * args.iters / (ms24 / 1000) / 1e9, "unit": "GTEPS", "ms_per_step": ms24,
+                  "vertices": g24.V, "edges": g24.E, "kernel_ms": k24,
+                  "achieved_gbs": b24 / (k24 / 1000) / 1e9, "frac": b24 / (k24 / 1000) / 1e9 / peak}
+        del g24
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         s, wall_cpu, threads, kind = cpu_pagerank(g, args.cpu_iters)
@@ -414,13 +453,12 @@ def run_gx(args, rank, local_rank, world):
                          f"({s:.2f} s of superstep time, {wall_cpu:.2f} s wall)"}
 
     if rank == 0:
-        cfg = base_config(args, g)
-        cfg.update({"parallelism": f"replicas{world}", "graph_build_s": round(build_s, 2),
-                    "graph_build": "on the GPU (gx_rmat_csc_gpu), identical to the host build"})
         line = {"metric": "pagerank_gteps", "value": value, "unit": "GTEPS", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded R-MAT)",
-                "config": cfg,
+                "config": base_config(args, g, world),
+                "graph_build": {"s": round(build_s, 2), "by": "on the GPU (gx_rmat_csc_gpu), identical to the "
+                                                              "host build and to the oracle's"},
                 "e2e": {"value": e2e_eps / 1e9, "unit": "GTEPS",
                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "s_per_step": e2e_step,
                         "step": "gx_load_csc from host arrays + gx_run (20 supersteps) + gx_get_values into a "
@@ -431,7 +469,7 @@ def run_gx(args, rank, local_rank, world):
                              "kernel": "pull_kernel<PAGERANK_REF>", "kernel_ms": pull_ms,
                              "algorithmic_bytes_per_launch": alg_bytes},
                 "cpu_baseline": cpu, "clocks": clocks, "wall_s_timed": wall, "sssp": sssp,
-                "iterations_per_step": iters_done / args.steps}
+                "rmat24": rmat24, "iterations_per_step": iters_done / args.steps}
         print(json.dumps(line), flush=True)
     eng.close()
     if dist is not None:
@@ -519,7 +557,8 @@ def run_batch(args):
     n = len(vb) - 1
     with gx.Engine() as e:
         e.load(g)
-        table = ROOT / "profiles" / "batch_autotune_table.jsonl"
+        # Every candidate schedule's time, beside the run's other outputs.
+        table = Path(os.environ.get("GX_AUTOTUNE_TABLE", tempfile.gettempdir())) / "gx_batch_autotune_table.jsonl"
         best, best_ms = e.batch_autotune(vb, pr_iters=30, cc_max_iter=1000, table_path=str(table))
         for _ in range(args.warmup):
             e.batch_run(vb, 30, 1000, tuning=best)

@@ -782,7 +782,37 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   if constexpr (APP == K_SSSP_UNIT || APP == K_SSSP_W || APP == K_CC) {
     if (c.async_mode) pull = pull_kernel<APP, false, true>;
   }
-  const int grid_pull = occupancy_grid<APP>(e, reinterpret_cast<const void*>(pull));
+  int grid_pull = occupancy_grid<APP>(e, reinterpret_cast<const void*>(pull));
+  // Hot-source table (resident graphs): one CTA of kHotThreads per SM whose
+  // dynamic shared memory holds the values of sources [0, hot_n).
+  int threads_pull = kThreads;
+  size_t hot_smem = 0;
+  pa.hot_n = 0;
+  if constexpr (APP != K_INDEG) {
+    if (e->cfg.hot_vertices > 0 && !c.async_mode && e->all_resident) {
+      void (*hk)(PullArgs) = e->cfg.exact_order ? pull_kernel<APP, true, false, false, true>
+                                                : pull_kernel<APP, false, false, false, true>;
+      cudaFuncAttributes attr{};
+      GX_CUDA(cudaFuncGetAttributes(&attr, reinterpret_cast<const void*>(hk)));
+      int optin = 0;
+      GX_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, e->dev));
+      const int64_t cap = std::max<int64_t>(0, (static_cast<int64_t>(optin) - static_cast<int64_t>(attr.sharedSizeBytes) -
+                                                1024) / static_cast<int64_t>(sizeof(T)));
+      const int64_t n = std::min<int64_t>({static_cast<int64_t>(e->cfg.hot_vertices), V, cap}) & ~int64_t(3);
+      if (n > 0) {
+        hot_smem = static_cast<size_t>(n) * sizeof(T);
+        GX_CUDA(cudaFuncSetAttribute(reinterpret_cast<const void*>(hk), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(hot_smem)));
+        int per_sm = 0;
+        GX_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, reinterpret_cast<const void*>(hk), kHotThreads,
+                                                              hot_smem));
+        grid_pull = std::max(1, per_sm) * e->n_sm;
+        pull = hk;
+        threads_pull = kHotThreads;
+        pa.hot_n = static_cast<int32_t>(n);
+      }
+    }
+  }
   // Block layout (config.layout = 1): the TMA-staged block kernel.
   const bool use_blocks = e->cfg.layout == 1 && e->all_resident && e->blocks_ready && !e->cfg.exact_order &&
                           APP != K_INDEG && !c.async_mode &&
@@ -861,7 +891,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
     auto enqueue = [&](int i) -> gx_status {
       if (prof) GX_CUDA(cudaEventRecord(pev[2 * i], e->s_comp));
       if (use_blocks) pull_block_kernel<APP><<<grid_block, kBlockThreads, block_smem, e->s_comp>>>(ba);
-      else pull<<<grid_pull, kThreads, 0, e->s_comp>>>(pa);
+      else pull<<<grid_pull, threads_pull, hot_smem, e->s_comp>>>(pa);
       if (prof) GX_CUDA(cudaEventRecord(pev[2 * i + 1], e->s_comp));
       if (push_ok) push_kernel<APP><<<grid_push, kThreads, 0, e->s_comp>>>(qa);
       finalize_kernel<APP><<<grid_fin, kThreads, 0, e->s_comp>>>(fa);
@@ -1108,6 +1138,7 @@ void gx_config_default(gx_config* cfg) {
   cfg->layout = 0;
   cfg->push_edge_fraction = 0.5;
   cfg->compress_cache = 1;
+  cfg->hot_vertices = 0;
 }
 
 void gx_run_params_default(gx_run_params* p, gx_app app) {

@@ -91,6 +91,10 @@ struct PullArgs {
   const uint2* chdr;
   const uint32_t* cpay;
   const uint8_t* w8;
+  // Hot-source table (HOT launches): the values (PageRank: contributions)
+  // of sources [0, hot_n) are copied into shared memory at the start of the
+  // launch and gathered from there; the other gathers bypass L1.
+  int32_t hot_n;
 };
 
 struct PushArgs {
@@ -139,27 +143,48 @@ __device__ __forceinline__ uint32_t sat_add(uint32_t a, uint32_t b) {
 #define GX_GATHER_CG 0
 #endif
 
+// The value source u offers: from the shared-memory table when HOT and u is
+// one of its hot_n sources, else from global memory.  Both loads are issued
+// without a branch (the table read at a clamped index, the global read under
+// a predicate), so a lane keeps all of its gathers in flight; cache hints on
+// the global read (L1::no_allocate, L1::evict_first) measured 1.2-2x slower.
 // ASYNC (Gauss-Seidel, min apps only): values are read and written in one
 // buffer during the step, so gathers go through L2 (ld.cg), never the
 // read-only path.
-template <class T, bool ASYNC>
-__device__ __forceinline__ T ld_val(const T* p) {
-  if constexpr (ASYNC) return __ldcg(p);
-  else return __ldg(p);
+template <class T, bool ASYNC, bool HOT>
+__device__ __forceinline__ T gather(const T* src, const T* hot, int32_t hot_n, int32_t u) {
+  static_assert(sizeof(T) == 4, "4-byte values");
+  if constexpr (HOT) {
+    uint32_t r;
+    memcpy(&r, hot + (u < hot_n ? u : hot_n - 1), 4);
+    asm("{\n\t.reg .pred p;\n\tsetp.ge.s32 p, %1, %2;\n\t@p ld.global.nc.b32 %0, [%3];\n\t}"
+        : "+r"(r) : "r"(u), "r"(hot_n), "l"(src + u));
+    T x;
+    memcpy(&x, &r, 4);
+    return x;
+  } else if constexpr (ASYNC) {
+    return __ldcg(src + u);
+  } else {
+    return __ldg(src + u);
+  }
 }
 
-template <int APP, bool ASYNC = false>
+template <int APP, bool ASYNC = false, bool HOT = false>
 __device__ __forceinline__ typename AppTraits<APP>::T edge_value(const PullArgs& a, const void* src_val,
-                                                                 const float* src_con, int32_t u, uint32_t wt) {
+                                                                 const float* src_con, int32_t u, uint32_t wt,
+                                                                 const void* hot = nullptr) {
   if constexpr (is_pr<APP>()) {
-    if (GX_GATHER_CG) return __ldcg(src_con + u);
-    return __ldg(src_con + u);
+    if (GX_GATHER_CG && !HOT) return __ldcg(src_con + u);
+    return gather<float, false, HOT>(src_con, static_cast<const float*>(hot), a.hot_n, u);
   } else if constexpr (APP == K_SSSP_UNIT) {
-    return ld_val<int32_t, ASYNC>(static_cast<const int32_t*>(src_val) + u) + 1;  // sssp.cpp:43
+    return gather<int32_t, ASYNC, HOT>(static_cast<const int32_t*>(src_val), static_cast<const int32_t*>(hot),
+                                       a.hot_n, u) + 1;  // sssp.cpp:43
   } else if constexpr (APP == K_SSSP_W) {
-    return sat_add(ld_val<uint32_t, ASYNC>(static_cast<const uint32_t*>(src_val) + u), wt);
+    return sat_add(gather<uint32_t, ASYNC, HOT>(static_cast<const uint32_t*>(src_val),
+                                                static_cast<const uint32_t*>(hot), a.hot_n, u), wt);
   } else {
-    return ld_val<int32_t, ASYNC>(static_cast<const int32_t*>(src_val) + u);      // cc.cpp:42
+    return gather<int32_t, ASYNC, HOT>(static_cast<const int32_t*>(src_val), static_cast<const int32_t*>(hot),
+                                       a.hot_n, u);  // cc.cpp:42
   }
 }
 
@@ -304,8 +329,9 @@ __device__ __forceinline__ typename AppTraits<APP>::T identity() {
   else return T(0x7fffffff);
 }
 
+template <int NW = kWarps>
 __device__ __forceinline__ void flush_block(Ctl* ctl, const LocalAcc& la) {
-  __shared__ unsigned long long s_red[5][kWarps];
+  __shared__ unsigned long long s_red[5][NW];
   unsigned long long ch = warp_sum(la.changed), ed = warp_sum(la.edges), rs = warp_sum(la.resid),
                      dg = warp_sum(la.dangl), fe = warp_sum(la.fedges);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -319,7 +345,7 @@ __device__ __forceinline__ void flush_block(Ctl* ctl, const LocalAcc& la) {
   __syncthreads();
   if (threadIdx.x < 5) {
     unsigned long long t = 0;
-    for (int i = 0; i < kWarps; ++i) t += s_red[threadIdx.x][i];
+    for (int i = 0; i < NW; ++i) t += s_red[threadIdx.x][i];
     unsigned long long* dst = threadIdx.x == 0 ? &ctl->changed
                             : threadIdx.x == 1 ? &ctl->edges
                             : threadIdx.x == 2 ? &ctl->resid_fx
@@ -383,10 +409,10 @@ __device__ __forceinline__ uint4 load_w4(const PullArgs& a, int64_t k) {
 // Warp-cooperative reduction of the edge range [b, e) (all lanes call it with
 // the same range): lanes take 8 consecutive edges each per round, with
 // 128-bit loads; the per-lane partials are combined by a fixed xor tree.
-template <int APP, bool ASYNC = false, bool COMP = false>
+template <int APP, bool ASYNC = false, bool COMP = false, bool HOT = false>
 __device__ __forceinline__ typename AppTraits<APP>::T warp_reduce_range(const PullArgs& a, const void* src_val,
                                                                         const float* src_con, int64_t b, int64_t e,
-                                                                        int lane) {
+                                                                        int lane, const void* hot = nullptr) {
   typedef typename AppTraits<APP>::T T;
   T acc = identity<APP>();
   for (int64_t q = (b & ~3ll) + 4 * lane; q < e; q += 256) {
@@ -405,7 +431,8 @@ __device__ __forceinline__ typename AppTraits<APP>::T warp_reduce_range(const Pu
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
       const int64_t k = (j < 4 ? q : q2) + (j & 3);
-      vals[j] = (k >= b && k < e) ? edge_value<APP, ASYNC>(a, src_val, src_con, cs[j], ws[j]) : identity<APP>();
+      vals[j] = (k >= b && k < e) ? edge_value<APP, ASYNC, HOT>(a, src_val, src_con, cs[j], ws[j], hot)
+                                  : identity<APP>();
     }
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc = combine<APP>(acc, vals[j]);
@@ -419,13 +446,33 @@ __device__ __forceinline__ typename AppTraits<APP>::T warp_reduce_range(const Pu
 #define GX_PULL_MIN_BLOCKS 4
 #endif
 
-template <int APP, bool EXACT, bool ASYNC = false, bool COMP = false>
-__global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(PullArgs a) {
+// HOT launches run one CTA of kHotThreads per SM, whose dynamic shared
+// memory holds the hot-source table (a.hot_n values, a multiple of 4).
+constexpr int kHotThreads = 1024;
+template <bool HOT> constexpr int pull_threads() { return HOT ? kHotThreads : kThreads; }
+
+template <int APP, bool EXACT, bool ASYNC = false, bool COMP = false, bool HOT = false>
+__global__ void __launch_bounds__(pull_threads<HOT>(), HOT ? 1 : GX_PULL_MIN_BLOCKS) pull_kernel(PullArgs a) {
   typedef typename AppTraits<APP>::T T;
-  __shared__ __align__(16) T s_buf[EXACT ? kWarps : 1][EXACT ? kChunk : 4];
+  static_assert(!(HOT && ASYNC), "a Gauss-Seidel step changes the values the table would hold");
+  constexpr int NW = pull_threads<HOT>() / 32;
+  __shared__ __align__(16) T s_buf[EXACT ? NW : 1][EXACT ? kChunk : 4];
+  extern __shared__ __align__(16) unsigned char s_dyn[];
   Ctl* ctl = a.ctl;
   const int done = ctl->done, mode = ctl->mode;
   if (done || mode == MODE_PUSH) return;
+  const void* hot = nullptr;
+  if constexpr (HOT) {
+    // The current step's values of sources [0, hot_n) (PageRank: their
+    // contributions), read through L2 in 16-byte pieces.
+    const int4* src = reinterpret_cast<const int4*>(
+        is_pr<APP>() ? static_cast<const void*>(ctl->cur ? a.con[1] : a.con[0])
+                     : static_cast<const void*>(ctl->cur ? a.val[1] : a.val[0]));
+    int4* dst = reinterpret_cast<int4*>(s_dyn);
+    for (int i = threadIdx.x; i < (a.hot_n >> 2); i += pull_threads<HOT>()) dst[i] = __ldcg(src + i);
+    __syncthreads();
+    hot = s_dyn;
+  }
   ApplyCtx c;
   c.step = ctl->step;
   c.damping = ctl->damping;
@@ -454,7 +501,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
   // next queue with units left, or stops when none has any.
   const int U = a.u_end - a.u_begin;
   const int nq = U / 256 < 1 ? 1 : (U / 256 < kQueues ? U / 256 : kQueues);
-  const int gw = blockIdx.x * kWarps + wid;
+  const int gw = blockIdx.x * NW + wid;
   int q = gw % nq;
   for (;;) {
     const int qb = a.u_begin + static_cast<int>((static_cast<int64_t>(U) * q) / nq);
@@ -514,7 +561,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
         const int64_t b = vb + static_cast<int64_t>(wu.y) * kHeavyChunk;
         const int64_t e = ve < b + kHeavyChunk ? ve : b + kHeavyChunk;
         T acc = identity<APP>();
-        if constexpr (APP != K_INDEG) acc = warp_reduce_range<APP, ASYNC, COMP>(a, src_val, src_con, b, e, lane);
+        if constexpr (APP != K_INDEG) acc = warp_reduce_range<APP, ASYNC, COMP, HOT>(a, src_val, src_con, b, e, lane, hot);
         if (lane == 0) {
           la.edges += e - b;
           T* part = static_cast<T*>(a.partial);
@@ -598,7 +645,8 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                   const int64_t kk = q + e;
-                  x[e] = (kk >= E0 && kk < E1) ? edge_value<APP, ASYNC>(a, src_val, src_con, cs[e], ws[e]) : identity<APP>();
+                  x[e] = (kk >= E0 && kk < E1) ? edge_value<APP, ASYNC, HOT>(a, src_val, src_con, cs[e], ws[e], hot)
+                                                : identity<APP>();
                 }
                 store4(buf + 4 * (lane + 32 * j), x);
               }
@@ -647,7 +695,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
 #pragma unroll
               for (int j = 0; j < 8; ++j) {
                 const int64_t kk = k + j;
-                vals[j] = (kk >= beg && kk < lend) ? edge_value<APP, ASYNC>(a, src_val, src_con, cs[j], ws[j])
+                vals[j] = (kk >= beg && kk < lend) ? edge_value<APP, ASYNC, HOT>(a, src_val, src_con, cs[j], ws[j], hot)
                                                    : identity<APP>();
               }
 #pragma unroll
@@ -663,7 +711,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
             const int l = __ffs(m) - 1;
             const int64_t bl = __shfl_sync(0xffffffffu, beg, l);
             const int64_t el = __shfl_sync(0xffffffffu, end, l);
-            const T r = warp_reduce_range<APP, ASYNC, COMP>(a, src_val, src_con, bl, el, lane);
+            const T r = warp_reduce_range<APP, ASYNC, COMP, HOT>(a, src_val, src_con, bl, el, lane, hot);
             if (lane == l) acc = combine<APP>(acc, r);
           }
         }
@@ -677,7 +725,7 @@ __global__ void __launch_bounds__(kThreads, GX_PULL_MIN_BLOCKS) pull_kernel(Pull
       if (lane == 0) bitmap_set_tile(a.bm, vb, m);
     }
   }
-  flush_block(ctl, la);
+  flush_block<NW>(ctl, la);
 }
 
 // ---------------------------------------------------------------------------

@@ -86,6 +86,9 @@ typedef struct gx_config {
   double push_edge_fraction;   /* SSSP/CC with push_sparse: also push when the frontier's out-edges are
                                   at most this fraction of E (default 0.5; 0 = push only when the
                                   step is selective, as the reference schedules it) */
+  int32_t hot_vertices;        /* resident pull steps: sources [0, hot_vertices) are gathered from a
+                                  table in shared memory, filled at the start of each pull launch
+                                  (capped by the shared memory of one CTA; 0 = off, the default) */
 } gx_config;
 
 typedef struct gx_run_params {

@@ -374,3 +374,136 @@ extern "C" int gxo_ppr(int32_t V, const int64_t* off, const int32_t* col, const 
   memcpy(out, R.data(), n * sizeof(double));
   return 0;
 }
+
+// ---------------------------------------------------------------------------
+// Graph construction, restated so that the benchmark's reference arm builds
+// its input without the product library.  The generator is the library's
+// seeded R-MAT: edge i of (seed, scale, a, b, c) draws one 16-bit uniform per
+// level from the SplitMix64 finaliser (Steele, Lea and Flood, OOPSLA 2014)
+// applied to a per-edge key, four levels per 64-bit draw, and picks the
+// quadrant a = (row 0, col 0), b = (0, 1), c = (1, 0), d = (1, 1), row =
+// source.  The CSC keeps each destination's sources ascending and unique, as
+// GraphMP/tools/format_spark.py:111-157 produces them with scipy's
+// csr_matrix; the partition rule is format_spark.py:91-108.
+// ---------------------------------------------------------------------------
+namespace {
+
+uint64_t splitmix_final(uint64_t z) {
+  z += 0x9e3779b97f4a7c15ull;
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  return z ^ (z >> 31);
+}
+
+}  // namespace
+
+extern "C" int gxo_rmat_csc(int32_t scale, int64_t n, double a, double b, double c, uint64_t seed, int32_t drop_self,
+                            int32_t dedup, int32_t symmetric, int threads, int64_t* off, int32_t* col,
+                            int64_t* n_out) {
+  if (scale < 1 || scale > 30 || n < 0 || !off || !n_out || (n > 0 && !col)) return 1;
+  if (threads <= 0) threads = omp_get_max_threads();
+  const int64_t V = int64_t(1) << scale;
+  const uint32_t qa = static_cast<uint32_t>(std::llround(a * 65536.0));
+  const uint32_t qb = qa + static_cast<uint32_t>(std::llround(b * 65536.0));
+  const uint32_t qc = qb + static_cast<uint32_t>(std::llround(c * 65536.0));
+  const uint64_t base = splitmix_final(seed ^ 0x5ca1ab1e0ddba11ull);
+  auto edge = [&](int64_t i, uint32_t* s_out, uint32_t* d_out) {
+    const uint64_t key = base ^ (static_cast<uint64_t>(i) * 0xd1b54a32d192ed03ull);
+    uint32_t s = 0, d = 0;
+    for (int level = 0; level < scale; ++level) {
+      const uint64_t draw = splitmix_final(key + static_cast<uint64_t>(level / 4 + 1) * 0x9e3779b97f4a7c15ull);
+      const uint32_t x = static_cast<uint32_t>(draw >> (16 * (level % 4))) & 0xffffu;
+      const uint32_t bit = 1u << (scale - 1 - level);
+      if (x >= qa) {
+        if (x < qb) d |= bit;
+        else if (x < qc) s |= bit;
+        else s |= bit, d |= bit;
+      }
+    }
+    *s_out = s;
+    *d_out = d;
+  };
+  // The edges once, then in-degree counts (with the reverse direction when
+  // symmetric), the fill, and per destination a sort and deduplication.
+  std::vector<uint32_t> es(static_cast<size_t>(n)), ed(static_cast<size_t>(n));
+  std::vector<std::atomic<int64_t>> cnt(static_cast<size_t>(V));
+  for (auto& x : cnt) x.store(0, std::memory_order_relaxed);
+#pragma omp parallel for num_threads(threads) schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    uint32_t s, d;
+    edge(i, &s, &d);
+    es[i] = s;
+    ed[i] = d;
+    if (drop_self && s == d) continue;
+    cnt[d].fetch_add(1, std::memory_order_relaxed);
+    if (symmetric) cnt[s].fetch_add(1, std::memory_order_relaxed);
+  }
+  off[0] = 0;
+  for (int64_t v = 0; v < V; ++v) off[v + 1] = off[v] + cnt[v].load(std::memory_order_relaxed);
+#pragma omp parallel for num_threads(threads) schedule(static)
+  for (int64_t v = 0; v < V; ++v) cnt[v].store(off[v], std::memory_order_relaxed);
+#pragma omp parallel for num_threads(threads) schedule(static)
+  for (int64_t i = 0; i < n; ++i) {
+    const uint32_t s = es[i], d = ed[i];
+    if (drop_self && s == d) continue;
+    col[cnt[d].fetch_add(1, std::memory_order_relaxed)] = static_cast<int32_t>(s);
+    if (symmetric) col[cnt[s].fetch_add(1, std::memory_order_relaxed)] = static_cast<int32_t>(d);
+  }
+  std::vector<int64_t> kept(static_cast<size_t>(V));
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 4096)
+  for (int64_t v = 0; v < V; ++v) {
+    int32_t* lo = col + off[v];
+    int32_t* hi = col + off[v + 1];
+    std::sort(lo, hi);
+    kept[v] = dedup ? std::unique(lo, hi) - lo : hi - lo;
+  }
+  // Compact in order (kept[v] <= the old list length, so moves go left).
+  int64_t w = 0;
+  for (int64_t v = 0; v < V; ++v) {
+    const int64_t from = off[v];
+    if (w != from) memmove(col + w, col + from, sizeof(int32_t) * static_cast<size_t>(kept[v]));
+    off[v] = w;
+    w += kept[v];
+  }
+  off[V] = w;
+  *n_out = w;
+  return 0;
+}
+
+extern "C" int gxo_partition_bounds(int32_t V, const int64_t* off, int32_t P, int32_t* bounds) {
+  if (V < 0 || P < 1 || !off || !bounds) return 1;
+  const int64_t per = (off[V] + P - 1) / P;  // ceil(E/P), format_spark.py:91
+  bounds[0] = 0;
+  for (int32_t i = 1; i < P; ++i) {
+    // First vertex whose cumulative in-degree reaches per*i (format_spark.py:100-101).
+    const int64_t* it = std::lower_bound(off, off + V + 1, per * i);
+    bounds[i] = std::max(bounds[i - 1], static_cast<int32_t>(std::min<int64_t>(it - off, V)));
+  }
+  bounds[P] = V;
+  return 0;
+}
+
+extern "C" int gxo_out_degree(int32_t V, const int64_t* off, const int32_t* col, int threads, int32_t* outdeg) {
+  if (V < 0 || !off || !outdeg) return 1;
+  if (threads <= 0) threads = omp_get_max_threads();
+  std::vector<std::atomic<int32_t>> od(static_cast<size_t>(V));
+  for (auto& x : od) x.store(0, std::memory_order_relaxed);
+#pragma omp parallel for num_threads(threads) schedule(static)
+  for (int64_t k = 0; k < off[V]; ++k) od[col[k]].fetch_add(1, std::memory_order_relaxed);
+  for (int32_t v = 0; v < V; ++v) outdeg[v] = od[v].load(std::memory_order_relaxed);
+  return 0;
+}
+
+// SSSP weight of edge u -> v in [1, 255], a pure function of (seed, u, v).
+extern "C" int gxo_edge_weights(uint64_t seed, int32_t V, const int64_t* off, const int32_t* col, int threads,
+                                uint32_t* w) {
+  if (V < 0 || !off || (off[V] > 0 && (!col || !w))) return 1;
+  if (threads <= 0) threads = omp_get_max_threads();
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 4096)
+  for (int32_t v = 0; v < V; ++v)
+    for (int64_t k = off[v]; k < off[v + 1]; ++k) {
+      const uint64_t pair = (static_cast<uint64_t>(static_cast<uint32_t>(col[k])) << 32) | static_cast<uint32_t>(v);
+      w[k] = 1u + static_cast<uint32_t>(splitmix_final(seed ^ splitmix_final(pair)) % 255u);
+    }
+  return 0;
+}

@@ -47,6 +47,18 @@ uint64_t gxo_triangles(int32_t V, const int64_t* off, const int32_t* col, int th
 int gxo_ppr(int32_t V, const int64_t* off, const int32_t* col, const int32_t* outdeg, int32_t k,
             const int32_t* sources, int32_t iters, double restart, int threads, double* out);
 
+/* Seeded R-MAT graph as a CSC (the library's generator restated): n edges
+ * over 2^scale vertices, quadrant probabilities a, b, c; self-loops dropped
+ * when drop_self, duplicates when dedup, both directions kept when
+ * symmetric.  col holds n entries (2n when symmetric); *n_out = off[V]. */
+int gxo_rmat_csc(int32_t scale, int64_t n, double a, double b, double c, uint64_t seed, int32_t drop_self,
+                 int32_t dedup, int32_t symmetric, int threads, int64_t* off, int32_t* col, int64_t* n_out);
+/* Edge-balanced destination-range shards (GraphMP/tools/format_spark.py:91-108). */
+int gxo_partition_bounds(int32_t V, const int64_t* off, int32_t P, int32_t* bounds);
+int gxo_out_degree(int32_t V, const int64_t* off, const int32_t* col, int threads, int32_t* outdeg);
+/* Seeded SSSP weights in [1, 255] per CSC entry, a pure function of (seed, source, destination). */
+int gxo_edge_weights(uint64_t seed, int32_t V, const int64_t* off, const int32_t* col, int threads, uint32_t* w);
+
 #ifdef __cplusplus
 }
 #endif

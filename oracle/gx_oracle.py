@@ -33,6 +33,15 @@ def lib():
         L.gxo_triangles.argtypes = [I32, P, P, C.c_int]
         L.gxo_ppr.restype = C.c_int
         L.gxo_ppr.argtypes = [I32, P, P, P, I32, P, I32, C.c_double, C.c_int, P]
+        D, I64, U64 = C.c_double, C.c_int64, C.c_uint64
+        L.gxo_rmat_csc.restype = C.c_int
+        L.gxo_rmat_csc.argtypes = [I32, I64, D, D, D, U64, I32, I32, I32, C.c_int, P, P, P]
+        L.gxo_partition_bounds.restype = C.c_int
+        L.gxo_partition_bounds.argtypes = [I32, P, I32, P]
+        L.gxo_out_degree.restype = C.c_int
+        L.gxo_out_degree.argtypes = [I32, P, P, C.c_int, P]
+        L.gxo_edge_weights.restype = C.c_int
+        L.gxo_edge_weights.argtypes = [U64, I32, P, P, C.c_int, P]
         _lib = L
     return _lib
 
@@ -80,3 +89,68 @@ def ppr(V, off, col, outdeg, sources, iters, restart=0.15, threads=0):
     if rc != 0:
         raise RuntimeError("gxo_ppr failed")
     return out
+
+
+class Graph:
+    """A graph in the shard layout the engine takes: bounds[P+1], off[V+1],
+    col[E], outdeg[V] (and weights[E] when asked for)."""
+
+    def __init__(self, V, off, col, outdeg, P, bounds, weights=None):
+        self.V, self.off, self.col, self.outdeg, self.P, self.bounds = V, off, col, outdeg, P, bounds
+        self.weights = weights
+
+    @property
+    def E(self) -> int:
+        return int(self.off[-1])
+
+
+def rmat_graph(scale, edge_factor, seed, P=1, symmetric=False, a=0.57, b=0.19, c=0.19, weight_seed=None,
+               threads=0) -> Graph:
+    """The library's seeded R-MAT graph (self-loops and duplicates removed,
+    optionally symmetrised) built by the oracle alone, with P edge-balanced
+    shards and, when weight_seed is given, SSSP weights."""
+    V = 1 << scale
+    n = edge_factor * V
+    off = np.empty(V + 1, np.int64)
+    col = np.empty(max(2 * n if symmetric else n, 1), np.int32)
+    nout = C.c_int64(0)
+    rc = lib().gxo_rmat_csc(scale, n, a, b, c, seed & 0xFFFFFFFFFFFFFFFF, 1, 1, int(symmetric), threads, _p(off),
+                            _p(col), C.byref(nout))
+    if rc != 0:
+        raise RuntimeError("gxo_rmat_csc failed")
+    col = col[:nout.value].copy()
+    outdeg = np.empty(V, np.int32)
+    bounds = np.empty(P + 1, np.int32)
+    if lib().gxo_out_degree(V, _p(off), _p(col), threads, _p(outdeg)) != 0 or \
+            lib().gxo_partition_bounds(V, _p(off), P, _p(bounds)) != 0:
+        raise RuntimeError("oracle graph construction failed")
+    g = Graph(V, off, col, outdeg, P, bounds)
+    if weight_seed is not None:
+        w = np.empty(max(g.E, 1), np.uint32)
+        if lib().gxo_edge_weights(weight_seed & 0xFFFFFFFFFFFFFFFF, V, _p(off), _p(col), threads, _p(w)) != 0:
+            raise RuntimeError("gxo_edge_weights failed")
+        g.weights = w[:g.E]
+    return g
+
+
+def write_shards(g: Graph, directory: str) -> str:
+    """Writes the graph as the reference's shard directory: {p}.edge.npy =
+    int32 [E_p, len(indices), len(indptr), start, end, indices..., indptr...]
+    for each destination range (GraphMP/tools/format_spark.py:137-157, read
+    by GraphMP/system/Comp.h:33-42), vertexout.npy and vertexin.npy (int32[V],
+    GraphMP/system/GraphPS.h:162-169)."""
+    import os
+    d = str(directory)
+    if not d.endswith("/"):
+        d += "/"
+    os.makedirs(d, exist_ok=True)
+    for p in range(g.P):
+        s, e = int(g.bounds[p]), int(g.bounds[p + 1])
+        lo, hi = int(g.off[s]), int(g.off[e])
+        indices = g.col[lo:hi].astype(np.int32)
+        indptr = (g.off[s:e + 1] - lo).astype(np.int32)
+        head = np.array([hi - lo, len(indices), len(indptr), s, e], np.int32)
+        np.save(f"{d}{p}.edge.npy", np.concatenate([head, indices, indptr]).astype(np.int32))
+    np.save(f"{d}vertexout.npy", np.ascontiguousarray(g.outdeg, np.int32))
+    np.save(f"{d}vertexin.npy", np.diff(g.off).astype(np.int32))
+    return d

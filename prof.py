@@ -1,5 +1,5 @@
 """Runs one workload of the engine and nothing else, so a profiler sees only
-its kernels:  python -m graphee_gb300.prof --app pagerank --scale 22 --iters 3
+its kernels:  python prof.py --app pagerank --scale 22 --iters 3
 
 Graph: seeded R-MAT (a,b,c=.57,.19,.19), edge factor 16, 256 shards, the
 same generator and seed as bench.py.

@@ -1,9 +1,13 @@
 """bench.py's measurement plumbing, on CPU: the nvidia-smi clock summary
 (samples kept inside the timed regions, throttle reasons collected), the
-DRAM traffic figures read from the committed ncu summaries, and the
+DRAM traffic figures read from the committed ncu summaries, the
 summaries' own hygiene (each names the command that made it, and every ncu
-command leaves the GPU clocks alone)."""
+command leaves the GPU clocks alone), and the reference arm (built and run
+without this package's library, on the GPU arm's workload)."""
+import json
 import re
+import subprocess
+import sys
 import time
 from pathlib import Path
 
@@ -64,9 +68,7 @@ def test_traffic_read_from_committed_profiles():
 def test_profile_summaries_name_their_commands():
     for p in sorted(ROOT.glob("profiles/*")):
         text = p.read_text()
-        assert p.suffix in (".md", ".txt", ".jsonl"), p.name
-        if p.suffix == ".jsonl":
-            continue
+        assert p.suffix in (".md", ".txt"), p.name
         assert re.search(r"[Cc]ommand", text), p.name
         joined = text.replace("\\\n", " ")             # shell line continuations
         for cmd in re.findall(r"ncu\b[^\n]*", joined):
@@ -74,3 +76,30 @@ def test_profile_summaries_name_their_commands():
                 continue                   # reading a report, or prose naming the tool
             assert "--clock-control none" in cmd, (p.name, cmd[:120])
         assert "/root/" not in text and "_work/" not in text, p.name
+
+
+def test_reference_arm_runs_without_the_library():
+    """The reference arm's graph comes from the oracle; the process never
+    imports graphee_gb300 nor maps libgx.so, and its config is the GPU arm's."""
+    code = (
+        "import runpy, sys, os\n"
+        "sys.argv = ['bench.py', '--impl', 'reference', '--scale', '14', '--steps', '1', '--warmup', '0']\n"
+        "try:\n"
+        "    runpy.run_path('bench.py', run_name='__main__')\n"
+        "except SystemExit:\n"
+        "    pass\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "print('LIB', any(m.startswith('graphee_gb300') for m in sys.modules), 'libgx.so' in maps)\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = r.stdout.strip().splitlines()
+    assert lines[-1] == "LIB False False", lines[-1]
+    line = json.loads(lines[0])
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["cpu_baseline"]["kind"] in ("port", "reference")
+    import graphee_gb300 as gx
+    g = gx.rmat_graph(14, 16, seed=bench.SEED, P=bench.SHARDS)
+
+    class A:
+        scale, edge_factor, iters = 14, 16, 20
+    assert line["config"] == bench.base_config(A, g, 1)
