@@ -44,7 +44,7 @@ class Config(C.Structure):
                 ("selective_threshold", C.c_double), ("heavy_degree", C.c_int32), ("tile_edges", C.c_int32),
                 ("exact_order", C.c_int32),
                 ("push_sparse", C.c_int32), ("use_graph", C.c_int32), ("wait_limit", C.c_uint32),
-                ("verbose", C.c_int32), ("profile", C.c_int32), ("layout", C.c_int32),
+                ("verbose", C.c_int32), ("profile", C.c_int32),
                 ("compress_cache", C.c_int32), ("push_edge_fraction", C.c_double), ("hot_vertices", C.c_int32)]
 
 
@@ -109,6 +109,7 @@ def lib() -> C.CDLL:
         "gx_last_error": (C.c_char_p, []),
         "gx_create": (C.c_int, [P, P]),
         "gx_destroy": (C.c_int, [P]),
+        "gx_set_wait_limit": (C.c_int, [P, C.c_uint32]),
         "gx_release_cached_memory": (C.c_int, [I32]),
         "gx_build_csc_gpu": (C.c_int, [I32, I32, I64, P, P, I32, P, P, P]),
         "gx_rmat_csc_gpu": (C.c_int, [I32, I32, I64, D, D, D, U64, I32, P, P, P]),
@@ -383,6 +384,11 @@ class Engine:
 
     def __exit__(self, *exc):
         self.close()
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Polls a device-side wait makes before the call gives up with
+        GX_ERR_TIMEOUT (config.wait_limit)."""
+        _check(lib().gx_set_wait_limit(self._h, polls), "gx_set_wait_limit")
 
     def load(self, g: Graph) -> "Engine":
         _check(lib().gx_load_csc(self._h, g.V, g.P, _ptr(g.bounds), _ptr(g.off), _ptr(g.col), _ptr(g.outdeg)),

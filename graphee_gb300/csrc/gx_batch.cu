@@ -387,7 +387,7 @@ gx_status batch_prepare(gx_engine* e, int32_t n, const int32_t* vbeg, BatchDev& 
   a.ctr = d.ctr;
   a.team = d.team;
   a.abort = d.abort;
-  a.spin_limit = 1u << 24;  // polls of at least 64 ns: over a second
+  a.spin_limit = e->cfg.wait_limit;  // polls of at least 64 ns each
   a.pr0 = d.pr0;
   a.pr1 = d.pr1;
   a.con0 = d.con0;

@@ -174,152 +174,6 @@ void build_units(gx_engine* e) {
   e->n_partials = n_part[P];
 }
 
-// ---- block layout of the default resident pull path (gx_block.cuh) ----
-
-// Copies, block by block, the per-edge array `src` (in CSC order) into the
-// block layout `dst`, zero-padding each block to its copied length.
-template <class U>
-void fill_block_layout(const gx_engine* e, const U* src, U* dst) {
-  const int64_t nb = static_cast<int64_t>(e->blocks.size());
-#pragma omp parallel for schedule(dynamic, 64)
-  for (int64_t i = 0; i < nb; ++i) {
-    const BlockDesc& d = e->blocks[i];
-    int64_t pos = d.e_begin;
-    if (d.type < 2) {
-      for (int j = 0; j < d.count; ++j) {
-        const int32_t v = e->b_vlist[d.first + j];
-        const int64_t n = e->off[v + 1] - e->off[v];
-        if (n) memcpy(dst + pos, src + e->off[v], sizeof(U) * n);
-        pos += n;
-      }
-    } else {
-      const int32_t v = e->b_heavy[d.first].x;
-      const int64_t b = e->off[v] + static_cast<int64_t>(d.aux) * kBlockEdges;
-      memcpy(dst + pos, src + b, sizeof(U) * d.n_real);
-      pos += d.n_real;
-    }
-    for (; pos < d.e_begin + d.n_copy; ++pos) dst[pos] = U(0);
-  }
-}
-
-gx_status build_blocks(gx_engine* e, const int32_t* h_col) {
-  const int32_t P = e->P;
-  const int64_t* off = e->off.data();
-  const int64_t heavy_thr = std::min<int64_t>(std::max(e->cfg.heavy_degree, kLightDegree + 1), kBlockEdges);
-  struct Proto {
-    int type;
-    int64_t edges;
-    std::vector<int32_t> verts;  // light/medium
-    int32_t hv = -1, chunk = 0, nch = 0;
-  };
-  std::vector<std::vector<Proto>> per(P);
-#pragma omp parallel for schedule(dynamic, 1)
-  for (int32_t p = 0; p < P; ++p) {
-    std::vector<Proto>& out = per[p];
-    Proto lb{0, 0, {}}, mb{1, 0, {}};
-    std::vector<int32_t> heavy;
-    for (int32_t v = e->bounds[p]; v < e->bounds[p + 1]; ++v) {
-      const int64_t d = off[v + 1] - off[v];
-      if (d <= kLightDegree) {
-        if (lb.verts.size() == static_cast<size_t>(kBlockVerts) || lb.edges + d > kBlockEdges) {
-          out.push_back(std::move(lb));
-          lb = Proto{0, 0, {}};
-        }
-        lb.verts.push_back(v);
-        lb.edges += d;
-      } else if (d <= heavy_thr) {
-        if (mb.verts.size() == static_cast<size_t>(kBlockVerts) || mb.edges + d > kBlockEdges) {
-          out.push_back(std::move(mb));
-          mb = Proto{1, 0, {}};
-        }
-        mb.verts.push_back(v);
-        mb.edges += d;
-      } else {
-        heavy.push_back(v);
-      }
-    }
-    if (!lb.verts.empty()) out.push_back(std::move(lb));
-    if (!mb.verts.empty()) out.push_back(std::move(mb));
-    for (int32_t v : heavy) {
-      const int64_t d = off[v + 1] - off[v];
-      const int32_t nch = static_cast<int32_t>((d + kBlockEdges - 1) / kBlockEdges);
-      for (int32_t c = 0; c < nch; ++c) {
-        Proto h{2, std::min<int64_t>(kBlockEdges, d - static_cast<int64_t>(c) * kBlockEdges), {}};
-        h.hv = v;
-        h.chunk = c;
-        h.nch = nch;
-        out.push_back(std::move(h));
-      }
-    }
-  }
-  e->blocks.clear();
-  e->b_vlist.clear();
-  e->b_loff.clear();
-  e->b_heavy.clear();
-  int64_t epos = 0, partials = 0;
-  for (int32_t p = 0; p < P; ++p) {
-    for (Proto& pr : per[p]) {
-      BlockDesc d{};
-      d.e_begin = epos;
-      d.n_real = static_cast<int>(pr.edges);
-      d.n_copy = static_cast<int>((pr.edges + 3) & ~3ll);
-      d.type = pr.type;
-      d.shard = p;
-      if (pr.type < 2) {
-        d.first = static_cast<int>(e->b_vlist.size());
-        d.count = static_cast<int>(pr.verts.size());
-        int64_t lo = 0;
-        for (int32_t v : pr.verts) {
-          e->b_vlist.push_back(v);
-          e->b_loff.push_back(static_cast<int32_t>(lo));
-          lo += off[v + 1] - off[v];
-        }
-        while (e->b_vlist.size() & 3) {
-          e->b_vlist.push_back(0);
-          e->b_loff.push_back(0);
-        }
-      } else {
-        if (pr.chunk == 0) {
-          e->b_heavy.push_back(make_int4(pr.hv, pr.nch, static_cast<int32_t>(partials), p));
-          partials += pr.nch;
-        }
-        d.first = static_cast<int>(e->b_heavy.size()) - 1;
-        d.count = pr.nch;
-        d.aux = pr.chunk;
-      }
-      e->blocks.push_back(d);
-      epos += d.n_copy;
-    }
-  }
-  e->b_edges = epos;
-  e->b_partials = partials;
-  std::vector<int32_t> colp(static_cast<size_t>(epos) + 4, 0);
-  fill_block_layout<int32_t>(e, h_col, colp.data());
-  const size_t nb = e->blocks.size();
-  GX_TRY(dev_alloc(&e->d_blocks, std::max<size_t>(nb, 1)));
-  GX_TRY(dev_alloc(&e->d_colp, colp.size()));
-  GX_TRY(dev_alloc(&e->d_vlist, e->b_vlist.size() + 4));
-  GX_TRY(dev_alloc(&e->d_loff, e->b_loff.size() + 4));
-  GX_TRY(dev_alloc(&e->d_bheavy, e->b_heavy.size() + 1));
-  {
-    uint32_t* pp = nullptr;
-    GX_TRY(dev_alloc(&pp, static_cast<size_t>(partials) + 1));
-    e->d_bpartial = pp;
-  }
-  GX_TRY(dev_alloc(&e->d_bticket, e->b_heavy.size() + 1));
-  if (nb) GX_CUDA(cudaMemcpy(e->d_blocks, e->blocks.data(), sizeof(BlockDesc) * nb, cudaMemcpyHostToDevice));
-  GX_CUDA(cudaMemcpy(e->d_colp, colp.data(), sizeof(int32_t) * colp.size(), cudaMemcpyHostToDevice));
-  if (!e->b_vlist.empty()) {
-    GX_CUDA(cudaMemcpy(e->d_vlist, e->b_vlist.data(), sizeof(int32_t) * e->b_vlist.size(), cudaMemcpyHostToDevice));
-    GX_CUDA(cudaMemcpy(e->d_loff, e->b_loff.data(), sizeof(int32_t) * e->b_loff.size(), cudaMemcpyHostToDevice));
-  }
-  if (!e->b_heavy.empty())
-    GX_CUDA(cudaMemcpy(e->d_bheavy, e->b_heavy.data(), sizeof(int4) * e->b_heavy.size(), cudaMemcpyHostToDevice));
-  GX_CUDA(cudaMemset(e->d_bticket, 0, sizeof(unsigned int) * (e->b_heavy.size() + 1)));
-  e->blocks_ready = true;
-  return GX_OK;
-}
-
 gx_status alloc_ctl(gx_engine* e) {
   if (!e->d_ctl) GX_TRY(dev_alloc(&e->d_ctl, 1));
   if (!e->h_ctl) GX_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->h_ctl), sizeof(Ctl), cudaHostAllocDefault));
@@ -813,37 +667,6 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
       }
     }
   }
-  // Block layout (config.layout = 1): the TMA-staged block kernel.
-  const bool use_blocks = e->cfg.layout == 1 && e->all_resident && e->blocks_ready && !e->cfg.exact_order &&
-                          APP != K_INDEG && !c.async_mode &&
-                          (APP != K_SSSP_W || e->d_wp != nullptr);
-  BlockArgs ba{};
-  int grid_block = 0;
-  const size_t block_smem = (2 * static_cast<size_t>(block_stage_bytes<APP>()) + kBlockEdges * 4) * kBlockWarps;
-  if (use_blocks) {
-    GX_CUDA(cudaFuncSetAttribute(pull_block_kernel<APP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 static_cast<int>(block_smem)));
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, pull_block_kernel<APP>, kBlockThreads, block_smem);
-    grid_block = std::max(1, per_sm) * e->n_sm;
-    ba.ctl = e->d_ctl;
-    ba.blocks = e->d_blocks;
-    ba.n_blocks = static_cast<int>(e->blocks.size());
-    ba.colp = e->d_colp;
-    ba.wp = e->d_wp;
-    ba.vlist = e->d_vlist;
-    ba.loff = e->d_loff;
-    ba.heavy = e->d_bheavy;
-    ba.outdeg = e->d_outdeg;
-    ba.val[0] = e->d_val[0];
-    ba.val[1] = e->d_val[1];
-    ba.con[0] = e->d_con[0];
-    ba.con[1] = e->d_con[1];
-    ba.partial = e->d_bpartial;
-    ba.hticket = e->d_bticket;
-    ba.bm = e->d_bm;
-    GX_CUDA(cudaMemsetAsync(e->d_bticket, 0, sizeof(unsigned int) * (e->b_heavy.size() + 1), e->s_comp));
-  }
   const int grid_push = occupancy_grid<APP>(e, reinterpret_cast<const void*>(push_kernel<APP>));
   const int grid_fin = std::max(1, std::min(e->n_sm * 4, (e->n_words + kThreads - 1) / kThreads));
 
@@ -890,8 +713,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
         });
     auto enqueue = [&](int i) -> gx_status {
       if (prof) GX_CUDA(cudaEventRecord(pev[2 * i], e->s_comp));
-      if (use_blocks) pull_block_kernel<APP><<<grid_block, kBlockThreads, block_smem, e->s_comp>>>(ba);
-      else pull<<<grid_pull, threads_pull, hot_smem, e->s_comp>>>(pa);
+      pull<<<grid_pull, threads_pull, hot_smem, e->s_comp>>>(pa);
       if (prof) GX_CUDA(cudaEventRecord(pev[2 * i + 1], e->s_comp));
       if (push_ok) push_kernel<APP><<<grid_push, kThreads, 0, e->s_comp>>>(qa);
       finalize_kernel<APP><<<grid_fin, kThreads, 0, e->s_comp>>>(fa);
@@ -1079,7 +901,11 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   float ms = 0;
   GX_CUDA(cudaEventElapsedTime(&ms, ev0, ev1));
 
-  if (e->h_ctl->error == 2) return fail(GX_ERR_CUDA, "gx_run: push frontier overflow");
+  // The superstep kernels raise one error: a push frontier that outgrew its
+  // buffer (impossible by construction, checked on every write).
+  if (e->h_ctl->error != 0)
+    return fail(GX_ERR_CUDA, "gx_run: device error %d (%s)", e->h_ctl->error,
+                e->h_ctl->error == 2 ? "push frontier overflow" : "unknown");
   GX_TRY(checkpoint(*e->h_ctl));
   const int32_t steps = e->h_ctl->step;
   e->last_steps = steps;
@@ -1132,10 +958,9 @@ void gx_config_default(gx_config* cfg) {
   cfg->exact_order = 0;
   cfg->push_sparse = 1;
   cfg->use_graph = 1;
-  cfg->wait_limit = 1u << 22;
+  cfg->wait_limit = 1u << 24;
   cfg->verbose = 0;
   cfg->profile = 0;
-  cfg->layout = 0;
   cfg->push_edge_fraction = 0.5;
   cfg->compress_cache = 1;
   cfg->hot_vertices = 0;
@@ -1171,6 +996,7 @@ gx_status gx_create(const gx_config* cfg, gx_engine** out) {
   if (c.device < 0 || c.device >= n) return fail(GX_ERR_INVALID, "device %d out of range [0,%d)", c.device, n);
   if (!(c.push_edge_fraction >= 0.0 && c.push_edge_fraction <= 1.0))
     return fail(GX_ERR_INVALID, "push_edge_fraction %g outside [0,1]", c.push_edge_fraction);
+  if (c.wait_limit == 0) return fail(GX_ERR_INVALID, "wait_limit must be at least 1");
   std::unique_ptr<gx_engine> e(new gx_engine());
   e->cfg = c;
   e->dev = c.device;
@@ -1193,6 +1019,12 @@ gx_status gx_create(const gx_config* cfg, gx_engine** out) {
 gx_status gx_destroy(gx_engine* e) {
   if (!e) return GX_OK;
   delete e;
+  return GX_OK;
+}
+
+gx_status gx_set_wait_limit(gx_engine* e, uint32_t polls) {
+  if (!e || polls == 0) return fail(GX_ERR_INVALID, "gx_set_wait_limit: engine NULL or limit 0");
+  e->cfg.wait_limit = polls;
   return GX_OK;
 }
 
@@ -1387,7 +1219,6 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   if (!direct) GX_TRY(build_signatures(e));
   phase("signatures");
   if (e->all_resident) {
-    if (e->cfg.layout == 1) GX_TRY(build_blocks(e, src_col));
     if (e->h_col) cudaFreeHost(e->h_col);
     e->h_col = nullptr;
   }
@@ -1420,12 +1251,6 @@ gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
     GX_CUDA(cudaMemsetAsync(e->d_w + e->E, 0, 8 * sizeof(uint32_t), e->s_copy));
     GX_TRY(upload_async(e, e->d_w, w, sizeof(uint32_t) * static_cast<size_t>(e->E), e->s_copy));
     GX_CUDA(cudaStreamSynchronize(e->s_copy));
-    if (e->blocks_ready) {
-      std::vector<uint32_t> wp(static_cast<size_t>(e->b_edges) + 4, 0u);
-      fill_block_layout<uint32_t>(e, w, wp.data());
-      GX_TRY(dev_alloc(&e->d_wp, wp.size()));
-      GX_CUDA(cudaMemcpy(e->d_wp, wp.data(), sizeof(uint32_t) * wp.size(), cudaMemcpyHostToDevice));
-    }
     e->out_built = false;
     return GX_OK;
   }
@@ -1462,12 +1287,6 @@ gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
     }
   } else {
     GX_TRY(plan_shards(e, e->h_col, false));
-  }
-  if (e->all_resident && e->blocks_ready) {
-    std::vector<uint32_t> wp(static_cast<size_t>(e->b_edges) + 4, 0u);
-    fill_block_layout<uint32_t>(e, w, wp.data());
-    GX_TRY(dev_alloc(&e->d_wp, wp.size()));
-    GX_CUDA(cudaMemcpy(e->d_wp, wp.data(), sizeof(uint32_t) * wp.size(), cudaMemcpyHostToDevice));
   }
   if (e->all_resident) {
     cudaFreeHost(e->h_w);

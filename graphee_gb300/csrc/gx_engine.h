@@ -10,7 +10,6 @@
 
 #include "gx_internal.h"
 #include "gx_kernels.cuh"
-#include "gx_block.cuh"
 
 #define GX_CUDA(call)                                                                                   \
   do {                                                                                                  \
@@ -200,22 +199,6 @@ struct gx_engine {
   int32_t n_work = 0;
   int32_t shard_group = 1;
 
-  // Block layout of the default resident pull path (gx_block.cuh).
-  bool blocks_ready = false;
-  std::vector<gx::BlockDesc> blocks;
-  std::vector<int32_t> b_vlist, b_loff;
-  std::vector<int4> b_heavy;
-  int64_t b_edges = 0;
-  int64_t b_partials = 0;
-  gx::BlockDesc* d_blocks = nullptr;
-  int32_t* d_colp = nullptr;
-  uint32_t* d_wp = nullptr;
-  int32_t* d_vlist = nullptr;
-  int32_t* d_loff = nullptr;
-  int4* d_bheavy = nullptr;
-  void* d_bpartial = nullptr;
-  unsigned int* d_bticket = nullptr;
-
   std::vector<uint32_t> init_vals;
   bool has_init = false;
   bool device_init = false;          // next gx_run starts from d_val[0] as it is
@@ -257,15 +240,6 @@ struct gx_engine {
     gx::dev_free(&d_ow);
     gx::dev_free(&d_stats);
     gx::dev_free(&d_work);
-    gx::dev_free(&d_blocks);
-    gx::dev_free(&d_colp);
-    gx::dev_free(&d_wp);
-    gx::dev_free(&d_vlist);
-    gx::dev_free(&d_loff);
-    gx::dev_free(&d_bheavy);
-    gx::dev_free(&d_bpartial);
-    gx::dev_free(&d_bticket);
-    blocks_ready = false;
     for (auto p : slot_col) gx::pool_free(p);
     for (auto p : slot_w) gx::pool_free(p);
     for (auto p : slot_blob) gx::pool_free(p);

@@ -52,7 +52,9 @@ std::mutex g_setup_mu;
 NoAllocScratch* g_scratch_addr[64] = {};
 
 // Device address of the scratch on the current device; looked up once per
-// device (with that device current) and cached.
+// device (with that device current) and cached for the life of the process.
+// cudaDeviceReset destroys the module instance the cached address points
+// into, so the entry point must not be called after a reset.
 gx_status scratch_on_current_device(NoAllocScratch** out) {
   int dev = 0;
   cudaError_t err = cudaGetDevice(&dev);
@@ -100,6 +102,23 @@ __global__ void noalloc_setup_kernel(NoAllocScratch* s, int32_t V, int32_t max_i
   for (int i = tid; i < 4; i += nt) s->hticket[i] = 0;
 }
 
+// The caller's CSC, checked before any kernel indexes with it: off[0] == 0,
+// off non-decreasing, off[V] == num_edges and every source id in [0, V).
+// A failure marks the run done with error 3, so the pull and finalize
+// launches queued behind this one return at once.
+__global__ void noalloc_validate_kernel(NoAllocScratch* s, const int64_t* off, const int32_t* col, int32_t V,
+                                        int64_t E) {
+  const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+  const int64_t nt = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  bool bad = tid == 0 && (off[0] != 0 || off[V] != E);
+  for (int64_t v = tid; v < V && !bad; v += nt) bad = off[v] > off[v + 1];
+  for (int64_t k = tid; k < E && !bad; k += nt) bad = col[k] < 0 || col[k] >= V;
+  if (bad) {
+    atomicOr(&s->ctl.error, 3);
+    s->ctl.done = 1;
+  }
+}
+
 // The final ranks sit in whichever buffer the last swap left current.
 __global__ void noalloc_result_kernel(NoAllocScratch* s, float* rank, int32_t V) {
   if (s->ctl.cur == 0) return;
@@ -140,6 +159,7 @@ extern "C" gx_status gx_pagerank_noalloc(const int64_t* d_off, const int32_t* d_
   const int grid_fin = std::max(1, std::min(n_sm * 4, (n_words + kThreads - 1) / kThreads));
 
   noalloc_setup_kernel<<<std::max(1, std::min(n_sm * 4, (U + 255) / 256)), 256, 0, cs>>>(s, V, max_iter, damping);
+  noalloc_validate_kernel<<<n_sm * 4, 256, 0, cs>>>(s, d_off, d_col, V, num_edges);
   init_kernel<K_PR_REF><<<n_sm * 4, 256, 0, cs>>>(&s->ctl, d_rank, s->con[0], d_outdeg, V, 0, 0);
 
   PullArgs pa{};
@@ -183,11 +203,16 @@ extern "C" gx_status gx_pagerank_noalloc(const int64_t* d_off, const int32_t* d_
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return fail(GX_ERR_CUDA, "gx_pagerank_noalloc: launch failed: %s", cudaGetErrorString(err));
   if (iterations_out) {
-    int32_t steps = 0;
-    err = cudaMemcpyAsync(&steps, &s->ctl.step, sizeof(int32_t), cudaMemcpyDeviceToHost, cs);
+    Ctl c{};
+    err = cudaMemcpyAsync(&c, &s->ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, cs);
     if (err == cudaSuccess) err = cudaStreamSynchronize(cs);
     if (err != cudaSuccess) return fail(GX_ERR_CUDA, "gx_pagerank_noalloc: %s", cudaGetErrorString(err));
-    *iterations_out = steps;
+    *iterations_out = c.step;
+    if (c.error == 3)
+      return fail(GX_ERR_INVALID,
+                  "gx_pagerank_noalloc: the CSC failed its device-side checks (off[0] == 0, off non-decreasing, "
+                  "off[V] == num_edges, source ids in [0, V)); no superstep ran");
+    if (c.error != 0) return fail(GX_ERR_CUDA, "gx_pagerank_noalloc: device error %d", c.error);
   }
   return GX_OK;
 }

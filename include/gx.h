@@ -73,11 +73,11 @@ typedef struct gx_config {
                                   vertices above heavy_degree (default 0) */
   int32_t push_sparse;         /* SSSP/CC: push over out-edges when selective (default 1) */
   int32_t use_graph;           /* replay the iteration loop as a CUDA graph (default 1) */
-  uint32_t wait_limit;         /* iteration cap of every device spin-wait (default 1<<22) */
+  uint32_t wait_limit;         /* polls (each of at least 64 ns) a device-side wait makes before it gives
+                                  up and the call returns GX_ERR_TIMEOUT; bounds the CTA-team barrier
+                                  of gx_batch_run (default 1<<24, over a second) */
   int32_t verbose;             /* per-iteration log lines on stderr (default 0) */
   int32_t profile;             /* time every pull launch with CUDA events (default 0) */
-  int32_t layout;              /* resident pull layout: 0 = warp work units (default), 1 = TMA-staged
-                                  blocks (edges re-laid per shard, cp.async.bulk double buffering) */
   int32_t compress_cache;      /* with a budget the plain shards exceed: keep every shard compressed
                                   (source ids as per-32-edge byte offsets from their minimum, weights as
                                   bytes when all fit), in HBM while the budget lasts and streamed
@@ -145,6 +145,10 @@ const char* gx_last_error(void);
 
 gx_status gx_create(const gx_config* cfg, gx_engine** out);
 gx_status gx_destroy(gx_engine* e);
+
+/* Changes the engine's config.wait_limit (>= 1) for its later calls.  No
+ * reference counterpart: the reference has no device-side waits. */
+gx_status gx_set_wait_limit(gx_engine* e, uint32_t polls);
 
 /* Engines draw device memory from a per-device pool that keeps blocks after
  * gx_destroy, so the next engine's load maps no new memory.  This returns
@@ -294,8 +298,15 @@ gx_status gx_pagerank_warm(gx_engine* e, gx_mlp* m, int32_t max_iter, double tol
  * num_edges + 4 entries (col_capacity; the last four are read but unused),
  * d_outdeg int32[V]; d_rank float[V] receives the ranks.  All device
  * pointers; `stream` is a cudaStream_t (NULL = legacy default stream).
+ * The CSC must satisfy off[0] == 0, off non-decreasing, off[V] == num_edges
+ * and 0 <= d_col[k] < V; a kernel checks this on the device before any other
+ * kernel indexes with it and, when it fails, no superstep runs.  Only a call
+ * that passes iterations_out waits for the result and then returns
+ * GX_ERR_INVALID for such a CSC (with *iterations_out = 0).
  * The first call on each device looks up the scratch's device address with
- * that device current; make that first call before any stream capture.
+ * that device current and caches it for the life of the process; make that
+ * first call before any stream capture, and do not call this entry point
+ * after cudaDeviceReset on that device (the cached address is then stale).
  * Every call reuses the same scratch and resets it first, so calls that may
  * overlap on the GPU (other streams, other host threads) race with each
  * other and must be serialised by the caller.  iterations_out (nullable)

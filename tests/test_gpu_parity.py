@@ -53,33 +53,6 @@ def test_pagerank_default_mode_vs_reference(golden_cases):
         e.close()
 
 
-def test_block_layout_vs_reference(golden_cases):
-    """The TMA-staged block layout (config.layout = 1): SSSP/CC bit-exact,
-    PageRank bit-exact wherever no vertex has more than 512 in-edges (every
-    list up to 512 is folded in edge order), else within tolerance."""
-    for name, c in golden_cases.items():
-        g = golden_graph(c)
-        for app, key, kw, iters in [(gx.APP_PAGERANK_REF, "pr", {}, 20), (gx.APP_SSSP, "sssp0", {"source": 0}, 200),
-                                    (gx.APP_CC, "cc", {}, 200)]:
-            with engine_for(g, layout=1) as e:
-                st = e.run(app, iters, **kw)
-                vals = e.values()
-                assert np.array_equal(run_changed(e, st["iterations"]), c[f"{key}_changed"]) or app == gx.APP_PAGERANK_REF
-            if app == gx.APP_PAGERANK_REF and np.diff(g.off).max() > 512:
-                assert np.abs(vals.astype(np.float64) - c[key]).max() / c[key].max() < 1e-3, name
-            else:
-                assert np.array_equal(vals.view(np.uint32), c[key].view(np.uint32)), (name, key)
-    g = gx.rmat_graph(15, 16, seed=7, P=8, weight_seed=99)
-    ref, _, _ = O.run(O.SSSP, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 1000, weights=g.weights, source=0)
-    with engine_for(g, layout=1) as e:
-        e.run(gx.APP_SSSP, 1000, source=0, weighted=True)
-        assert np.array_equal(e.values(), ref)
-        e.run(gx.APP_PAGERANK_REF, 20)
-        pr = e.values().astype(np.float64)
-    pref, _, _ = O.run(O.PAGERANK_REF, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 20)
-    assert np.abs(pr - pref).max() / pref.max() < 1e-5
-
-
 @pytest.mark.parametrize("push", [1, 0])
 @pytest.mark.parametrize("source", [1, 0])
 def test_sssp_unit_bitexact_vs_reference(golden_cases, push, source):
