@@ -92,13 +92,18 @@ def build_apps() -> Path:
     return APP
 
 
+# Where the build looks for the reference tree (read only, to compile the
+# reference's own apps as the oracle's pin); GX_REFERENCE_ROOT overrides it.
+REFERENCE_MOUNT = "/root/reference"
+
+
 def build_oracle() -> None:
     """Compiles the oracle's CPU restatement; and the reference's own apps
     when the reference tree is present on this machine."""
     r = subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "oracle"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
-    ref_root = os.environ.get("GX_REFERENCE_ROOT", "/root/reference")
+    ref_root = os.environ.get("GX_REFERENCE_ROOT", REFERENCE_MOUNT)
     if Path(ref_root, "GraphMP", "system", "Comp.h").exists():
         r = subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF={ref_root}"],
                            capture_output=True, text=True)

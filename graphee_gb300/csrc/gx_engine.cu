@@ -588,7 +588,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   GX_CUDA(cudaMemsetAsync(e->d_work, 0, sizeof(unsigned int) * e->n_work, e->s_comp));
   GX_CUDA(cudaMemsetAsync(e->d_hticket, 0, sizeof(unsigned int) * std::max<size_t>(e->heavy.size(), 1), e->s_comp));
 
-  PullArgs pa{};
+  PullArgs pa;
+  memset(&pa, 0, sizeof(pa));  // every byte defined: the args are part of the graph cache key
   pa.ctl = e->d_ctl;
   pa.off = e->d_off;
   pa.col = e->d_col;
@@ -608,7 +609,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   pa.ctr = e->d_work;
   pa.heavy_deg = e->cfg.exact_order ? INT32_MAX : std::max(e->cfg.heavy_degree, 32);
   pa.bm = e->d_bm;
-  PushArgs qa{};
+  PushArgs qa;
+  memset(&qa, 0, sizeof(qa));
   qa.ctl = e->d_ctl;
   qa.ooff = e->d_ooff;
   qa.ocol = e->d_ocol;
@@ -619,7 +621,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   qa.frontier = e->d_frontier;
   qa.ctr = e->d_work + kQueues;
   qa.bm = e->d_bm;
-  FinArgs fa{};
+  FinArgs fa;
+  memset(&fa, 0, sizeof(fa));
   fa.ctl = e->d_ctl;
   fa.stats = e->d_stats;
   fa.bm = e->d_bm;
@@ -725,19 +728,40 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
     // Profiling times each pull launch with its own events, so it launches
     // directly instead of replaying a graph.
     if (e->cfg.use_graph && !prof && !every) {
-      cudaGraph_t graph;
-      GX_CUDA(cudaStreamBeginCapture(e->s_comp, cudaStreamCaptureModeThreadLocal));
-      for (int i = 0; i < K; ++i) {
-        gx_status st = enqueue(i);
-        if (st != GX_OK) {
-          cudaStreamEndCapture(e->s_comp, &graph);
-          return st;
+      // A replay bakes in kernels, launch shapes and arguments only, so an
+      // executable graph captured by an earlier run with the same bytes of
+      // all three is replayed again instead of captured anew.
+      GraphKey key;
+      memset(&key, 0, sizeof(key));
+      key.app = APP;
+      key.k = K;
+      key.push = push_ok;
+      key.pull = reinterpret_cast<const void*>(pull);
+      key.grid_pull = grid_pull;
+      key.threads_pull = threads_pull;
+      key.smem_pull = hot_smem;
+      key.grid_push = grid_push;
+      key.grid_fin = grid_fin;
+      key.pa = pa;
+      key.qa = qa;
+      key.fa = fa;
+      exec = e->cached_graph(key);
+      if (!exec) {
+        cudaGraph_t graph;
+        GX_CUDA(cudaStreamBeginCapture(e->s_comp, cudaStreamCaptureModeThreadLocal));
+        for (int i = 0; i < K; ++i) {
+          gx_status st = enqueue(i);
+          if (st != GX_OK) {
+            cudaStreamEndCapture(e->s_comp, &graph);
+            return st;
+          }
         }
+        GX_CUDA(cudaStreamEndCapture(e->s_comp, &graph));
+        cudaError_t err = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (err != cudaSuccess) return fail(GX_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(err));
+        e->keep_graph(key, exec);
       }
-      GX_CUDA(cudaStreamEndCapture(e->s_comp, &graph));
-      cudaError_t err = cudaGraphInstantiate(&exec, graph, 0);
-      cudaGraphDestroy(graph);
-      if (err != cudaSuccess) return fail(GX_ERR_CUDA, "cudaGraphInstantiate: %s", cudaGetErrorString(err));
       launches = 0;
     }
     const int per_step = push_ok ? 3 : 2;
@@ -751,10 +775,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
       }
       GX_CUDA(cudaMemcpyAsync(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->s_comp));
       cudaError_t err = cudaStreamSynchronize(e->s_comp);
-      if (err != cudaSuccess) {
-        if (exec) cudaGraphExecDestroy(exec);
-        return fail(GX_ERR_CUDA, "superstep loop: %s", cudaGetErrorString(err));
-      }
+      if (err != cudaSuccess) return fail(GX_ERR_CUDA, "superstep loop: %s", cudaGetErrorString(err));
       const int ran = std::min(K, e->h_ctl->step - steps_before);
       for (int i = 0; i < ran && prof; ++i) {
         float t = 0;
@@ -775,7 +796,6 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
         GX_CUDA(cudaStreamSynchronize(e->s_comp));
       }
     }
-    if (exec) cudaGraphExecDestroy(exec);
   } else {
     // Host-driven steps: one launch per shard, streamed shards through the
     // slot ring on the copy stream, overlapped with compute.  A Jacobi step

@@ -108,6 +108,19 @@ struct UninitAlloc : std::allocator<T> {
 template <class T>
 using hvec = std::vector<T, UninitAlloc<T>>;
 
+// What a captured superstep graph depends on: the kernels, their launch
+// shapes and their argument bytes (zero-filled before use, padding included).
+struct GraphKey {
+  int app, k, push;
+  const void* pull;
+  int grid_pull, threads_pull;
+  size_t smem_pull;
+  int grid_push, grid_fin;
+  PullArgs pa;
+  PushArgs qa;
+  FinArgs fa;
+};
+
 inline int app_kind(const gx_run_params& p) {
   switch (p.app) {
     case GX_APP_PAGERANK_REF: return K_PR_REF;
@@ -212,6 +225,23 @@ struct gx_engine {
   std::vector<gx::StepStats> last_stats;
   gx_run_stats last_run{};
 
+  // Executable superstep graphs of earlier runs, keyed by GraphKey bytes.
+  std::vector<std::pair<gx::GraphKey, cudaGraphExec_t>> graphs;
+
+  cudaGraphExec_t cached_graph(const gx::GraphKey& k) const {
+    for (const auto& g : graphs)
+      if (memcmp(&g.first, &k, sizeof(k)) == 0) return g.second;
+    return nullptr;
+  }
+  void keep_graph(const gx::GraphKey& k, cudaGraphExec_t x) {
+    if (graphs.size() >= 16) drop_graphs();
+    graphs.emplace_back(k, x);
+  }
+  void drop_graphs() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    graphs.clear();
+  }
+
   ~gx_engine() { release(); }
 
   void release_graph() {
@@ -266,6 +296,7 @@ struct gx_engine {
   void release() {
     cudaSetDevice(dev);
     release_graph();
+    drop_graphs();
     gx::dev_free(&d_ctl);
     if (h_ctl) cudaFreeHost(h_ctl);
     h_ctl = nullptr;

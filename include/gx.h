@@ -75,7 +75,8 @@ typedef struct gx_config {
   int32_t use_graph;           /* replay the iteration loop as a CUDA graph (default 1) */
   uint32_t wait_limit;         /* polls (each of at least 64 ns) a device-side wait makes before it gives
                                   up and the call returns GX_ERR_TIMEOUT; bounds the CTA-team barrier
-                                  of gx_batch_run (default 1<<24, over a second) */
+                                  of gx_batch_run and the grid barrier of gx_ppr (default 1<<24, over
+                                  a second) */
   int32_t verbose;             /* per-iteration log lines on stderr (default 0) */
   int32_t profile;             /* time every pull launch with CUDA events (default 0) */
   int32_t compress_cache;      /* with a budget the plain shards exceed: keep every shard compressed
@@ -204,9 +205,12 @@ gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_stats* stats);
 
 /* Personalized PageRank for k <= 64 sources at once, as one sparse x dense
  * product per step over the loaded CSC: R <- restart*S + (1-restart)*A^T
- * D^-1 R, R0 = S (one-hot columns), dangling mass dropped, FP32.  No
- * reference counterpart (PageRank's pull, pagerank.cpp:44-48, on k vectors).
- * host_out (nullable) receives R as float[V][k], row-major. */
+ * D^-1 R, R0 = S (one-hot columns), dangling mass dropped, FP32.  Every step
+ * runs in one persistent launch (a grid barrier between steps, bounded by
+ * config.wait_limit: GX_ERR_TIMEOUT when it gives up), replayed as a CUDA
+ * graph; rows are k rounded up to 8 columns.  No reference counterpart
+ * (PageRank's pull, pagerank.cpp:44-48, on k vectors).  host_out (nullable)
+ * receives R as float[V][k], row-major. */
 gx_status gx_ppr(gx_engine* e, int32_t k, const int32_t* sources, int32_t iters, double restart,
                  float* host_out, gx_run_stats* stats);
 

@@ -260,7 +260,7 @@ def test_triangle_count_empty_graph():
         assert e.triangle_count()[0] == 0
 
 
-@pytest.mark.parametrize("k", [64, 5])
+@pytest.mark.parametrize("k", [64, 8, 5, 1])
 def test_ppr_vs_fp64(k):
     g = gx.rmat_graph(13, 16, seed=17, P=4)
     rng = np.random.default_rng(k)
@@ -274,6 +274,7 @@ def test_ppr_vs_fp64(k):
     assert np.abs(R - ref).max() < 1e-6
     assert np.all(np.abs(R - ref).sum(axis=0) < 1e-5 * np.maximum(1.0, ref.sum(axis=0)))
     assert st["iterations"] == 15
+    assert st["kernel_launches"] == 2          # one init kernel, one persistent launch for all 15 steps
 
 
 def _instance(g, vb, i):
@@ -388,3 +389,22 @@ def test_graph_without_edges(budget):
             st = e.run(app, 50, **kw)
             assert np.array_equal(e.values().view(np.uint32), ref.view(np.uint32)), app
             assert np.array_equal(run_changed(e, st["iterations"]), ch), app
+
+
+def test_cached_superstep_graphs_follow_the_loaded_graph():
+    """gx_run replays an executable graph captured by an earlier run with the
+    same kernels, launch shapes and argument bytes.  Runs of different apps
+    and lengths, and a second graph of the same size loaded into the same
+    engine, all match the oracle."""
+    g1 = gx.rmat_graph(14, 16, seed=61, P=8, weight_seed=3)
+    g2 = gx.rmat_graph(14, 16, seed=62, P=8, weight_seed=4)
+    with gx.Engine(exact_order=1) as e:
+        for g in (g1, g2, g1):
+            e.load(g)
+            for iters in (20, 5, 20):
+                e.run(gx.APP_PAGERANK_REF, iters)
+                ref, _, _ = O.run(O.PAGERANK_REF, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, iters)
+                assert np.array_equal(e.values().view(np.uint32), ref.view(np.uint32)), iters
+            e.run(gx.APP_SSSP, 1000, source=0, weighted=True)
+            ref, _, _ = O.run(O.SSSP, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 1000, weights=g.weights, source=0)
+            assert np.array_equal(e.values(), ref)

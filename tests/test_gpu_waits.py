@@ -1,9 +1,9 @@
 """Bounded device-side waits, driven to their limit without faulting or
-hanging the GPU: the CTA-team barrier of the batched kernel polls at most
-config.wait_limit times; with a limit of one poll a team barrier gives up,
-every CTA leaves through the abort flag, and the call returns
-GX_ERR_TIMEOUT.  The same engine then runs the batch again with the normal
-limit and matches the oracle."""
+hanging the GPU: the CTA-team barrier of the batched kernel and the grid
+barrier of the persistent PPR launch poll at most config.wait_limit times;
+with a limit of one poll a barrier gives up, every CTA leaves through the
+abort flag, and the call returns GX_ERR_TIMEOUT.  The same engine then runs
+again with the normal limit and matches the oracle."""
 import numpy as np
 import pytest
 
@@ -51,3 +51,18 @@ def test_wait_limit_must_be_positive():
     with gx.Engine() as e:
         with pytest.raises(gx.GxError):
             e.set_wait_limit(0)
+
+
+def test_ppr_grid_barrier_timeout_then_recovery():
+    g = gx.rmat_graph(15, 16, seed=8, P=4)
+    src = np.array([0, 5, 77, 1000], np.int32)
+    with gx.Engine() as e:
+        e.load(g)
+        e.set_wait_limit(1)
+        with pytest.raises(gx.GxError) as ei:
+            e.ppr(src, 10)
+        assert ei.value.status == gx.GX_ERR_TIMEOUT
+        e.set_wait_limit(1 << 24)
+        R, st = e.ppr(src, 10)
+    ref = O.ppr(g.V, g.off, g.col, g.outdeg, src, 10, 0.15)
+    assert np.abs(R - ref).max() < 1e-6
