@@ -418,36 +418,37 @@ gx_status plan_shards(gx_engine* e, const int32_t* src_col, bool col_on_device) 
   return GX_OK;
 }
 
-// Per-vertex shard-group masks, built shard by shard (streamed shards go
-// through slot 0).
-gx_status build_signatures(gx_engine* e) {
-  const int32_t P = e->P;
-  e->sig_ready = false;
-  e->shard_group = (P + 63) / 64;
-  GX_TRY(dev_alloc(&e->d_sig, static_cast<size_t>(e->V)));
-  GX_CUDA(cudaMemsetAsync(e->d_sig, 0, sizeof(unsigned long long) * e->V, e->s_comp));
-  if (e->all_resident) {
-    // One launch over every edge; each finds its shard from the shards' edge ranges.
-    std::vector<int64_t> ebound(static_cast<size_t>(P) + 1);
-    for (int32_t p = 0; p <= P; ++p) ebound[p] = e->off[e->bounds[p]];
-    int64_t* d_eb = nullptr;
-    GX_TRY(dev_alloc(&d_eb, ebound.size()));
-    GX_CUDA(cudaMemcpy(d_eb, ebound.data(), sizeof(int64_t) * ebound.size(), cudaMemcpyHostToDevice));
-    signature_all_kernel<<<e->n_sm * 8, 256, 0, e->s_comp>>>(e->d_sig, e->d_col, d_eb, P, e->shard_group, e->V);
-    cudaError_t err = cudaGetLastError();
-    if (err == cudaSuccess) err = cudaStreamSynchronize(e->s_comp);
-    gx::pool_free(d_eb);
-    if (err != cudaSuccess) return fail(GX_ERR_CUDA, "signatures: %s", cudaGetErrorString(err));
-    e->sig_ready = true;
-    return GX_OK;
+// Streamed graphs: for every vertex, the set of shards it is a source in
+// (a bitset of P bits), kept in host memory, where the host-driven step loop
+// turns the changed vertices a finalize lists into the shards the next
+// selective step streams and sweeps.  Built once, on the GPU, shard by shard
+// (streamed shards go through slot 0), then copied to the host.
+__global__ void shard_sets_kernel(unsigned long long* sets, int words, const int32_t* col, int64_t e0, int64_t e1,
+                                  int32_t p) {
+  const int w = p >> 6;
+  const unsigned long long bit = 1ull << (p & 63);
+  for (int64_t k = e0 + blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < e1;
+       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
+    unsigned long long* x = sets + static_cast<int64_t>(col[k]) * words + w;
+    if (!(*x & bit)) atomicOr(x, bit);
   }
+}
+
+gx_status build_shard_sets(gx_engine* e) {
+  const int32_t P = e->P;
+  const int words = (P + 63) / 64;
+  unsigned long long* d_sets = nullptr;
+  GX_TRY(dev_alloc(&d_sets, static_cast<size_t>(e->V) * words));
+  struct Free {
+    unsigned long long* p;
+    ~Free() { gx::pool_free(p); }
+  } guard{d_sets};
+  GX_CUDA(cudaMemsetAsync(d_sets, 0, sizeof(unsigned long long) * e->V * words, e->s_comp));
   for (int32_t p = 0; p < P; ++p) {
     const int64_t e0 = e->off[e->bounds[p]], e1 = e->off[e->bounds[p + 1]];
     if (e1 == e0) continue;
     const int32_t* col = nullptr;
-    if (e->all_resident) {
-      col = e->d_col;
-    } else if (e->resident[p]) {
+    if (e->resident[p]) {
       col = e->d_col + e->dev_base[p];
     } else {
       const int64_t lo = e0 & ~3ll;
@@ -455,14 +456,16 @@ gx_status build_signatures(gx_engine* e) {
                               e->s_comp));
       col = e->slot_col[0] - lo;
     }
-    const unsigned long long bit = 1ull << (p / e->shard_group);
     const int64_t n = e1 - e0;
     const int grid = static_cast<int>(std::min<int64_t>((n + 255) / 256, static_cast<int64_t>(e->n_sm) * 8));
-    signature_kernel<<<grid, 256, 0, e->s_comp>>>(e->d_sig, col, e0, e1, bit);
+    shard_sets_kernel<<<grid, 256, 0, e->s_comp>>>(d_sets, words, col, e0, e1, p);
     GX_CUDA(cudaGetLastError());
   }
+  e->h_shard_sets.resize(static_cast<size_t>(e->V) * words);
+  GX_CUDA(cudaMemcpyAsync(e->h_shard_sets.data(), d_sets, sizeof(unsigned long long) * e->h_shard_sets.size(),
+                          cudaMemcpyDeviceToHost, e->s_comp));
   GX_CUDA(cudaStreamSynchronize(e->s_comp));
-  e->sig_ready = true;
+  e->shard_set_words = words;
   return GX_OK;
 }
 
@@ -526,11 +529,25 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   c.max_iter = prm.max_iter;
   c.n_vertices = V;
   c.n_shards = e->P;
-  c.shard_group = e->shard_group;
+  c.shard_words = (e->P + 31) / 32;
   c.push_ok = push_ok;
   c.push_edge_limit =
       push_ok ? static_cast<unsigned long long>(e->cfg.push_edge_fraction * static_cast<double>(e->E)) : 0ull;
-  c.sig = e->sig_ready ? e->d_sig : nullptr;
+  // Selective pull steps: resident graphs mark their shards on the device
+  // from the out-edge CSR (built for push, or at the first selective step);
+  // streamed graphs list their changed vertices for the host.
+  c.shard_bm = e->d_shard_bm;
+  c.bounds = e->d_bounds;
+  if (e->all_resident) {
+    c.mark_mode = e->out_built ? MARK_OUT : MARK_NONE;
+    c.ooff = e->d_ooff;
+    c.ocol = e->d_ocol;
+  } else {
+    c.mark_mode = MARK_LIST;
+    c.changed_list = e->d_changed_list;
+    c.changed_cap = static_cast<unsigned int>(e->changed_cap);
+  }
+  GX_CUDA(cudaMemsetAsync(e->d_shard_bm, 0, sizeof(uint32_t) * 2 * c.shard_words, e->s_comp));
   c.damping = prm.damping;
   c.inv_n = 1.0 / V;
   c.fx_scale = static_cast<double>(V) * 1073741824.0;  // 2^30 per 1/N of rank
@@ -541,7 +558,6 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   c.cur = 0;
   c.mode = MODE_DENSE;
   c.done = prm.max_iter <= 0;
-  c.shard_mask = ~0ull;
   // Initial values: init_vertex of the app, or the caller's values.
   int use_init = 0;
   if (e->device_init) {
@@ -696,6 +712,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   };
   int64_t h2d_bytes = 0;
   int32_t streamed = 0;
+  std::vector<int32_t> host_shards_active;  // streamed runs: shards each selective step swept
   int32_t launches = 1;  // init_kernel
   int32_t pull_launches = 0;
   double ms_pull = 0;
@@ -786,14 +803,22 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
       steps_before = e->h_ctl->step;
       GX_TRY(checkpoint(*e->h_ctl));
       if (e->h_ctl->done) break;
-      // Shard signatures are built the first time a step turns selective;
-      // until then selective steps sweep every shard.
-      if (!e->sig_ready && e->h_ctl->mode == MODE_SELECTIVE) {
-        GX_TRY(build_signatures(e));
-        const unsigned long long* sp = e->d_sig;
-        GX_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(e->d_ctl) + offsetof(Ctl, sig), &sp, sizeof(sp),
-                                cudaMemcpyHostToDevice, e->s_comp));
-        GX_CUDA(cudaStreamSynchronize(e->s_comp));
+      // Apps without push steps get the out-edge CSR that marks their
+      // selective steps' shards the first time a step turns selective; until
+      // then (and where vertexout.npy disagrees with the shards) a selective
+      // step sweeps every shard.
+      if (e->h_ctl->mark_mode == MARK_NONE && e->h_ctl->mode == MODE_SELECTIVE && !e->out_unbuildable) {
+        if (build_out_edges(e, false) == GX_OK) {
+          const int mm = MARK_OUT;
+          const void* ptrs[2] = {e->d_ooff, e->d_ocol};
+          GX_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(e->d_ctl) + offsetof(Ctl, mark_mode), &mm, sizeof(int),
+                                  cudaMemcpyHostToDevice, e->s_comp));
+          GX_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(e->d_ctl) + offsetof(Ctl, ooff), ptrs, sizeof(ptrs),
+                                  cudaMemcpyHostToDevice, e->s_comp));
+          GX_CUDA(cudaStreamSynchronize(e->s_comp));
+        } else {
+          e->out_unbuildable = true;
+        }
       }
     }
   } else {
@@ -826,6 +851,9 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
     GX_CUDA(cudaEventCreate(&k0));
     GX_CUDA(cudaEventCreate(&k1));
     int slot = 0;
+    host_shards_active.assign(static_cast<size_t>(std::max(prm.max_iter, 1)), -1);
+    std::vector<char> shard_on(static_cast<size_t>(e->P), 1);
+    std::vector<int32_t> changed;
     for (int step = prm.first_step; step < prm.max_iter; ++step) {
       GX_CUDA(cudaMemcpyAsync(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, e->s_comp));
       GX_CUDA(cudaStreamSynchronize(e->s_comp));
@@ -833,6 +861,30 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
       GX_TRY(checkpoint(hc));
       if (hc.done) break;
       const bool sel = hc.mode == MODE_SELECTIVE;
+      // A selective step streams and sweeps only the shards in which the
+      // last step's changed vertices are sources.
+      std::fill(shard_on.begin(), shard_on.end(), 1);
+      if (sel && !hc.list_overflow) {
+        if (e->shard_set_words == 0) GX_TRY(build_shard_sets(e));
+        const unsigned n = std::min<unsigned>(hc.n_changed_list, static_cast<unsigned>(e->changed_cap));
+        changed.resize(n);
+        if (n)
+          GX_CUDA(cudaMemcpyAsync(changed.data(), e->d_changed_list, sizeof(int32_t) * n, cudaMemcpyDeviceToHost,
+                                  e->s_comp));
+        GX_CUDA(cudaStreamSynchronize(e->s_comp));
+        const int words = e->shard_set_words;
+        std::vector<unsigned long long> m(words, 0ull);
+        for (int32_t u : changed)
+          for (int w = 0; w < words; ++w) m[w] |= e->h_shard_sets[static_cast<size_t>(u) * words + w];
+        int n_on = 0;
+        for (int32_t p = 0; p < e->P; ++p) n_on += shard_on[p] = (m[p >> 6] >> (p & 63)) & 1ull;
+        host_shards_active[hc.step] = n_on;
+      }
+      {
+        const unsigned int zero[2] = {0u, 0u};  // n_changed_list, list_overflow
+        GX_CUDA(cudaMemcpyAsync(reinterpret_cast<char*>(e->d_ctl) + offsetof(Ctl, n_changed_list), zero,
+                                sizeof(zero), cudaMemcpyHostToDevice, e->s_comp));
+      }
       GX_CUDA(cudaEventRecord(k0, e->s_comp));
       GX_CUDA(cudaEventRecord(c0, e->s_comp));
       for (const int32_t p : order) {
@@ -841,7 +893,7 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
         sp.u_end = e->unit_begin[p + 1];
         sp.ctr = e->d_work + 2 * kQueues + kQueues * p;
         if (sp.u_end == sp.u_begin) continue;
-        const bool active = !sel || ((hc.shard_mask >> (p / e->shard_group)) & 1ull);
+        const bool active = shard_on[p] != 0;
         const bool use_comp = e->comp && !e->resident[p] && active && e->cb_bytes[p] > 0;
         if (use_comp) {
           cudaStream_t cs = e->s_copies[slot % e->s_copies.size()];
@@ -858,9 +910,15 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
           sp.cpay = reinterpret_cast<const uint32_t*>(base + e->cb_pay[p]);
           sp.w8 = base + e->cb_w8[p] - 32 * e->cb_c0[p];
           ++streamed;
-        } else if (e->resident[p] || !active) {
+        } else if (e->resident[p]) {
           sp.col = e->d_col + e->dev_base[p];
           if (e->d_w) sp.w = e->d_w + e->dev_base[p];
+          sp.skip = !active;
+        } else if (!active) {
+          // Not streamed: the launch only carries the shard's values over.
+          sp.col = nullptr;
+          sp.w = nullptr;
+          sp.skip = 1;
         } else {
           const int64_t lo = e->off[e->bounds[p]] & ~3ll;
           const int64_t n = std::min<int64_t>((e->off[e->bounds[p + 1]] + 3) & ~3ll, e->E + 4) - lo;
@@ -932,6 +990,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   e->last_stats.assign(std::max(steps, 0), StepStats{});
   if (steps > 0)
     GX_CUDA(cudaMemcpy(e->last_stats.data(), e->d_stats, sizeof(StepStats) * steps, cudaMemcpyDeviceToHost));
+  for (int32_t i = 0; i < steps && i < static_cast<int32_t>(host_shards_active.size()); ++i)
+    if (host_shards_active[i] >= 0) e->last_stats[i].shards_active = host_shards_active[i];
   gx_run_stats rs{};
   rs.iterations = steps;
   for (const StepStats& s : e->last_stats) {
@@ -1116,7 +1176,6 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
     GX_CUDA(cudaMemsetAsync(scratch.flag, 0, sizeof(unsigned int), e->s_copy));
     validate_csc_kernel<<<e->n_sm * 8, 256, 0, e->s_copy>>>(e->d_off, V, e->d_col, E, scratch.flag);
     GX_CUDA(cudaGetLastError());
-    e->shard_group = (P + 63) / 64;  // signatures come later, at the first selective step
   }
   e->bounds.assign(bounds, bounds + P + 1);
   e->off.resize(static_cast<size_t>(V) + 1);
@@ -1236,8 +1295,16 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
     }
   }
   phase("edges");
-  if (!direct) GX_TRY(build_signatures(e));
-  phase("signatures");
+  // Shard bounds and bitmaps of the selective steps; the changed-vertex list
+  // that streamed graphs hand to the host (a selective step changes fewer
+  // than BF_THRE * V vertices).
+  GX_TRY(dev_alloc(&e->d_bounds, static_cast<size_t>(P) + 1));
+  GX_CUDA(cudaMemcpy(e->d_bounds, bounds, sizeof(int32_t) * (P + 1), cudaMemcpyHostToDevice));
+  GX_TRY(dev_alloc(&e->d_shard_bm, 2 * static_cast<size_t>((P + 31) / 32)));
+  if (!e->all_resident) {
+    e->changed_cap = std::max<int64_t>(4096, V / 256);
+    GX_TRY(dev_alloc(&e->d_changed_list, static_cast<size_t>(e->changed_cap)));
+  }
   if (e->all_resident) {
     if (e->h_col) cudaFreeHost(e->h_col);
     e->h_col = nullptr;
@@ -1295,7 +1362,10 @@ gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
       GX_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->h_col), (e->E + 8) * sizeof(int32_t), cudaHostAllocDefault));
       GX_CUDA(cudaMemcpy(e->h_col, e->d_col, (e->E + 8) * sizeof(int32_t), cudaMemcpyDeviceToHost));
       GX_TRY(plan_shards(e, e->h_col, false));
-      GX_TRY(build_signatures(e));
+      if (!e->all_resident && !e->d_changed_list) {
+        e->changed_cap = std::max<int64_t>(4096, e->V / 256);
+        GX_TRY(dev_alloc(&e->d_changed_list, static_cast<size_t>(e->changed_cap)));
+      }
       if (e->all_resident) {
         cudaFreeHost(e->h_col);
         e->h_col = nullptr;

@@ -196,8 +196,17 @@ struct gx_engine {
   unsigned int* d_hticket = nullptr;
   uint32_t* d_bm = nullptr;
   int32_t n_words = 0;
-  unsigned long long* d_sig = nullptr;
-  bool sig_ready = false;            // d_sig built (resident graphs build it at their first selective step)
+  // Selective steps: shard bounds (P+1), two shard bitmaps marked by the
+  // device (resident graphs), the changed-vertex list a streamed step hands
+  // to the host and the host's per-vertex shard sets (P bits per vertex,
+  // built at a streamed graph's first selective step).
+  int32_t* d_bounds = nullptr;
+  uint32_t* d_shard_bm = nullptr;
+  int32_t* d_changed_list = nullptr;
+  int64_t changed_cap = 0;
+  std::vector<unsigned long long> h_shard_sets;
+  int shard_set_words = 0;
+  bool out_unbuildable = false;      // vertexout.npy disagrees with the shards: no out-edge CSR
   int4* d_frontier = nullptr;
   unsigned long long frontier_cap = 0;
   int64_t* d_ooff = nullptr;
@@ -210,7 +219,6 @@ struct gx_engine {
   int32_t stats_cap = 0;
   unsigned int* d_work = nullptr;
   int32_t n_work = 0;
-  int32_t shard_group = 1;
 
   std::vector<uint32_t> init_vals;
   bool has_init = false;
@@ -262,8 +270,14 @@ struct gx_engine {
     gx::dev_free(&d_partial);
     gx::dev_free(&d_hticket);
     gx::dev_free(&d_bm);
-    gx::dev_free(&d_sig);
-    sig_ready = false;
+    gx::dev_free(&d_bounds);
+    gx::dev_free(&d_shard_bm);
+    gx::dev_free(&d_changed_list);
+    changed_cap = 0;
+    h_shard_sets.clear();
+    h_shard_sets.shrink_to_fit();
+    shard_set_words = 0;
+    out_unbuildable = false;
     gx::dev_free(&d_frontier);
     gx::dev_free(&d_ooff);
     gx::dev_free(&d_ocol);

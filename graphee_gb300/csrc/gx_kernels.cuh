@@ -35,19 +35,33 @@ struct StepStats {
   int mode;
 };
 
+// Which shards a selective step sweeps (the partition activation of
+// GraphPS.h:349-368, exact per shard instead of a bloom filter):
+enum MarkMode : int {
+  MARK_NONE = 0,     // selective steps sweep every shard
+  MARK_OUT = 1,      // finalize marks the shards of the changed vertices' out-neighbours (out-edge CSR)
+  MARK_LIST = 2      // finalize lists the changed vertices; the host marks their shards (streamed graphs)
+};
+
 // Control block.  Fields above `step` are set by the host before a run; the
 // rest evolve on the device.
 struct Ctl {
   int max_iter;
   int n_vertices;
   int n_shards;
-  int shard_group;          // shards per bit of the 64-bit shard mask
+  int shard_words;          // 32-bit words of one shard bitmap, (P + 31) / 32
   int push_ok;              // out-edges resident: sparse steps may push
   int step0_push;           // SSSP from init_vertex: step 0 pushes from the source alone
   int async_mode;           // min apps: pull updates values in place (no buffer swap)
-  int pad0;
+  int mark_mode;            // MarkMode
   unsigned long long push_edge_limit;  // push when the frontier has at most this many out-edges
-  const unsigned long long* sig;       // per-vertex shard-group masks, or null until built
+  uint32_t* shard_bm;       // MARK_OUT: two shard bitmaps of shard_words words; [shard_cur] is current
+  const int64_t* ooff;      // MARK_OUT: out-edge CSR and the shards' vertex bounds (P+1)
+  const int32_t* ocol;
+  const int32_t* bounds;
+  int32_t* changed_list;    // MARK_LIST: the changed vertices of the last step
+  unsigned int changed_cap;
+  int pad0;
   double damping;
   double inv_n;             // 1.0 / N, as the reference computes it
   double fx_scale;          // fixed-point scale of resid_fx / dangl_fx
@@ -61,8 +75,10 @@ struct Ctl {
   int n_frontier;           // frontier entries for the current push step
   int error;
   double base;              // PageRank STD: (1-d)/N + d*D/N of the current step
-  unsigned long long shard_mask;       // active shard groups, current step
-  unsigned long long shard_mask_next;  // being built by finalize
+  int shard_cur;            // MARK_OUT: index of the current step's shard bitmap
+  int shard_valid;          // MARK_OUT: the current bitmap was marked for this (selective) step
+  unsigned int n_changed_list;  // MARK_LIST: entries written (the host resets it)
+  int list_overflow;        // MARK_LIST: more changed vertices than changed_cap
   unsigned long long changed, active, edges, resid_fx, dangl_fx;  // current-step accumulators
   unsigned long long front_edges;      // out-edges of the vertices that changed this step
   unsigned int next_frontier;
@@ -93,8 +109,12 @@ struct PullArgs {
   const uint8_t* w8;
   // Hot-source table (HOT launches): the values (PageRank: contributions)
   // of sources [0, hot_n) are copied into shared memory at the start of the
-  // launch and gathered from there; the other gathers bypass L1.
+  // launch and gathered from there.
   int32_t hot_n;
+  // 1: a shard the step does not sweep (host-driven selective steps of
+  // streamed graphs): every unit only carries its vertices' values over, and
+  // no edge is read (col then points nowhere valid).
+  int32_t skip;
 };
 
 struct PushArgs {
@@ -481,8 +501,10 @@ __global__ void __launch_bounds__(pull_threads<HOT>(), HOT ? 1 : GX_PULL_MIN_BLO
   c.base = ctl->base;
   c.outdeg = ctl->push_ok ? a.outdeg : nullptr;
   const int cur = ctl->cur;
-  const int group = ctl->shard_group;
-  const unsigned long long smask = ctl->shard_mask;
+  // Selective steps skip the units of shards the last finalize left unmarked.
+  const uint32_t* sbm = (mode == MODE_SELECTIVE && ctl->shard_valid)
+                            ? ctl->shard_bm + static_cast<int64_t>(ctl->shard_cur) * ctl->shard_words
+                            : nullptr;
   // Ternaries, not a[cur]: indexing a parameter array with a runtime value
   // would copy the whole parameter block to local memory.
   const void* src_val = cur ? a.val[1] : a.val[0];
@@ -490,7 +512,7 @@ __global__ void __launch_bounds__(pull_threads<HOT>(), HOT ? 1 : GX_PULL_MIN_BLO
   void* dst_val = ASYNC ? const_cast<void*>(src_val) : (cur ? a.val[0] : a.val[1]);
   const float* src_con = cur ? a.con[1] : a.con[0];
   float* dst_con = cur ? a.con[0] : a.con[1];
-  const bool selective = mode == MODE_SELECTIVE;
+  const bool selective = sbm != nullptr;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   T* buf = s_buf[EXACT ? wid : 0];
   LocalAcc la;
@@ -540,7 +562,8 @@ __global__ void __launch_bounds__(pull_threads<HOT>(), HOT ? 1 : GX_PULL_MIN_BLO
     if (GX_TILE_PREFETCH) prefetch_tile(0);
     for (int j = 0; j < cnt; ++j) {
       const int2 wu = make_int2(__shfl_sync(0xffffffffu, myu.x, j), __shfl_sync(0xffffffffu, myu.y, j));
-      const bool on = !selective || ((smask >> (__shfl_sync(0xffffffffu, mysh, j) / group)) & 1ull);
+      const int jsh = __shfl_sync(0xffffffffu, mysh, j);
+      const bool on = !a.skip && (!selective || ((sbm[jsh >> 5] >> (jsh & 31)) & 1u));
       const int64_t cbeg = pbeg, cend = pend;
       const T cold = pold;
       const int32_t cod = pod;
@@ -823,7 +846,6 @@ template <int APP>
 __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
   typedef typename AppTraits<APP>::T T;
   __shared__ unsigned long long s_act[kWarps];
-  __shared__ unsigned long long s_mask[kWarps];
   __shared__ bool s_last;
   Ctl* ctl = a.ctl;
   const Ctl c = *ctl;
@@ -840,13 +862,16 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
   // reference's selective steps it is chosen when the frontier's out-edges
   // are few enough to beat a full pull.
   const bool push_next = c.push_ok && (sel_next || c.front_edges <= c.push_edge_limit);
-  // Without shard signatures (not built yet) a selective step sweeps every shard.
-  const unsigned long long* sig = c.sig;
-  const bool want_mask = sel_next && !push_next && sig != nullptr;
+  // A selective pull step sweeps only the shards its changed in-neighbours
+  // reach: marked here from the out-edges (MARK_OUT), or by the host from
+  // the list of changed vertices (MARK_LIST).  Without either, every shard.
+  const bool mark = sel_next && !push_next &&
+                    (c.mark_mode == MARK_LIST || (c.mark_mode == MARK_OUT && c.shard_bm != nullptr));
+  uint32_t* next_bm = c.shard_bm ? c.shard_bm + static_cast<int64_t>(c.shard_cur ^ 1) * c.shard_words : nullptr;
   const int nb = (c.mode == MODE_PUSH || c.async_mode) ? c.cur : (c.cur ^ 1);
   const T* newv = static_cast<const T*>(nb ? a.val[1] : a.val[0]);
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  unsigned long long act = 0, mask = 0;
+  unsigned long long act = 0;
   // Warp-uniform sweep: lane i takes word w0 + i, so the frontier compaction
   // can reserve its slots with one atomic per warp.
   for (int w0 = blockIdx.x * kThreads + (wid << 5); w0 < a.n_words; w0 += gridDim.x * kThreads) {
@@ -855,8 +880,27 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
     if (word) {
       a.bm[w] = 0;
       act += __popc(word);
-      if (want_mask) {
-        for (uint32_t x = word; x; x &= x - 1) mask |= sig[(w << 5) + __ffs(x) - 1];
+      if (mark) {
+        for (uint32_t x = word; x; x &= x - 1) {
+          const int u = (w << 5) + __ffs(x) - 1;
+          if (c.mark_mode == MARK_OUT) {
+            for (int64_t k = c.ooff[u]; k < c.ooff[u + 1]; ++k) {
+              const int v = c.ocol[k];
+              int lo = 0, hi = c.n_shards;  // bounds[lo] <= v < bounds[lo + 1]
+              while (hi - lo > 1) {
+                const int mid = (lo + hi) >> 1;
+                if (__ldg(c.bounds + mid) <= v) lo = mid;
+                else hi = mid;
+              }
+              const uint32_t bit = 1u << (lo & 31);
+              if (!(next_bm[lo >> 5] & bit)) atomicOr(next_bm + (lo >> 5), bit);
+            }
+          } else {
+            const unsigned pos = atomicAdd(&ctl->n_changed_list, 1u);
+            if (pos < c.changed_cap) c.changed_list[pos] = u;
+            else ctl->list_overflow = 1;
+          }
+        }
       }
     }
     if (push_next) {
@@ -891,21 +935,12 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
     }
   }
   act = warp_sum(act);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mask |= __shfl_xor_sync(0xffffffffu, mask, o);
-  if (lane == 0) {
-    s_act[wid] = act;
-    s_mask[wid] = mask;
-  }
+  if (lane == 0) s_act[wid] = act;
   __syncthreads();
   if (threadIdx.x == 0) {
-    unsigned long long ta = 0, tm = 0;
-    for (int i = 0; i < kWarps; ++i) {
-      ta += s_act[i];
-      tm |= s_mask[i];
-    }
+    unsigned long long ta = 0;
+    for (int i = 0; i < kWarps; ++i) ta += s_act[i];
     if (ta) atomicAdd(&ctl->active, ta);
-    if (tm) atomicOr(&ctl->shard_mask_next, tm);
     __threadfence();
     const unsigned ticket = atomicAdd(&ctl->fin_ticket, 1u);
     s_last = ticket == gridDim.x - 1;
@@ -922,16 +957,23 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
     s.resid_fx = vc->resid_fx;
     s.dangl_fx = vc->dangl_fx;
     s.mode = c.mode;
-    s.shards_active = c.mode == MODE_SELECTIVE ? __popcll(c.shard_mask) : -1;
+    s.shards_active = -1;  // every shard (the host counts MARK_LIST steps)
+    if (c.mode == MODE_SELECTIVE && c.shard_valid) {
+      const uint32_t* cur_bm = c.shard_bm + static_cast<int64_t>(c.shard_cur) * c.shard_words;
+      int n = 0;
+      for (int i = 0; i < c.shard_words; ++i) n += __popc(cur_bm[i]);
+      s.shards_active = n;
+    }
     a.stats[c.step] = s;
-    const unsigned long long next_mask = vc->shard_mask_next;
     const double resid = static_cast<double>(s.resid_fx) / c.fx_scale;
     int done = (s.changed == 0 && c.step > 1) || (c.step + 1 >= c.max_iter);  // GraphPS.h:256,383
     if (is_pr<APP>() && c.tolerance > 0 && resid < c.tolerance) done = 1;
     ctl->cur = nb;  // Msg <- MsgNew as a swap (in place: push steps, async mode)
     ctl->mode = push_next ? MODE_PUSH : (sel_next ? MODE_SELECTIVE : MODE_DENSE);
-    ctl->shard_mask = want_mask ? next_mask : ~0ull;
-    ctl->shard_mask_next = 0;
+    if (c.mark_mode == MARK_OUT) {
+      ctl->shard_valid = mark;
+      if (mark) ctl->shard_cur = c.shard_cur ^ 1;
+    }
     ctl->n_frontier = static_cast<int>(vc->next_frontier);
     ctl->next_frontier = 0;
     ctl->front_edges = 0;
@@ -950,6 +992,11 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
     ctl->done = done;
   }
   for (int i = threadIdx.x; i < a.n_work_ctr; i += kThreads) a.work_ctr[i] = 0;
+  // The bitmap the next finalize marks into starts empty.
+  if (c.mark_mode == MARK_OUT && mark) {
+    uint32_t* old_bm = c.shard_bm + static_cast<int64_t>(c.shard_cur) * c.shard_words;
+    for (int i = threadIdx.x; i < c.shard_words; i += kThreads) old_bm[i] = 0;
+  }
 }
 
 // Initial values (init_vertex of each app) and PageRank contributions.
@@ -969,38 +1016,6 @@ __global__ void init_kernel(Ctl* ctl, void* val, float* con, const int32_t* outd
       const int32_t od = outdeg[i];
       con[i] = v[i] / static_cast<float>(od > 0 ? od : 1);
     }
-  }
-}
-
-// Per-vertex shard-group masks: bit g of sig[u] is set iff u is a source in
-// a shard of group g.  Replaces the bloom-filter build (GraphPS.h:225-245).
-static __global__ void signature_kernel(unsigned long long* sig, const int32_t* col, int64_t e0, int64_t e1,
-                                 unsigned long long bit) {
-  for (int64_t k = e0 + blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < e1;
-       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    const int u = col[k];
-    if ((sig[u] & bit) == 0) atomicOr(sig + u, bit);
-  }
-}
-
-// The same masks for a fully resident graph in one launch: edge k belongs
-// to the shard whose edge range [ebound[p], ebound[p+1]) holds it.
-static __global__ void signature_all_kernel(unsigned long long* sig, const int32_t* col, const int64_t* ebound,
-                                            int32_t P, int32_t group, int32_t V) {
-  const int64_t E = ebound[P];
-  for (int64_t k = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; k < E;
-       k += static_cast<int64_t>(gridDim.x) * blockDim.x) {
-    int lo = 0, hi = P;  // ebound[lo] <= k < ebound[lo + 1]
-    while (hi - lo > 1) {
-      const int mid = (lo + hi) >> 1;
-      if (ebound[mid] <= k) lo = mid;
-      else hi = mid;
-    }
-    const unsigned long long bit = 1ull << (lo / group);
-    const int u = col[k];
-    // May run before the host has read the load-time checks: skip bad ids.
-    if (u < 0 || u >= V) continue;
-    if ((sig[u] & bit) == 0) atomicOr(sig + u, bit);
   }
 }
 

@@ -81,7 +81,7 @@ __global__ void noalloc_setup_kernel(NoAllocScratch* s, int32_t V, int32_t max_i
     c.max_iter = max_iter;
     c.n_vertices = V;
     c.n_shards = 1;
-    c.shard_group = 1;
+    c.shard_words = 1;
     c.push_ok = 0;
     c.damping = damping;
     c.inv_n = 1.0 / V;
@@ -89,7 +89,6 @@ __global__ void noalloc_setup_kernel(NoAllocScratch* s, int32_t V, int32_t max_i
     c.tolerance = 0;
     c.sel_threshold = 0.001;
     c.mode = MODE_DENSE;
-    c.shard_mask = ~0ull;
     s->ctl = c;
   }
   const int32_t U = (V + 31) / 32;

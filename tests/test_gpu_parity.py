@@ -358,8 +358,10 @@ def test_load_rejects_bad_csc(budget):
 def test_selective_steps_skip_shards_and_keep_values():
     """On a path the SSSP frontier is one vertex per step, far below BF_THRE:
     with push steps off, every step after the first few is selective, and
-    the shard-group masks (built at the first selective step) leave all but
-    one or two shards idle.  Values and per-step counts stay the reference's."""
+    once the out-edge CSR that marks shards is built (at the first selective
+    step, seen by the host after a replay of 8 steps) a step sweeps exactly
+    the one shard that holds the frontier's out-neighbour.  Values and
+    per-step counts stay the reference's."""
     V = 4096
     src = np.arange(V - 1, dtype=np.int32)
     off, col = gx.build_csc(V, src, src + 1)
@@ -371,8 +373,52 @@ def test_selective_steps_skip_shards_and_keep_values():
     assert np.array_equal(run_changed(e, st["iterations"]), ch)
     sel = [e.iter_stats(i) for i in range(st["iterations"]) if e.iter_stats(i)["mode"] == 1]
     assert len(sel) > V // 2
-    assert sum(m["shards_active"] <= 2 for m in sel) > len(sel) // 2
+    assert all(m["shards_active"] == 1 for m in sel[16:])
     e.close()
+
+
+def _frontier_shards(g, dist, t):
+    """Shards holding the out-neighbours of the vertices unit-weight SSSP
+    changes at step t - 1 (those at distance t)."""
+    dst = np.repeat(np.arange(g.V), np.diff(g.off))
+    src_at_t = dist[g.col] == t
+    return set((np.searchsorted(g.bounds, dst[src_at_t], side="right") - 1).tolist())
+
+
+@pytest.mark.parametrize("budget", [-1, "stream"])
+def test_selective_steps_sweep_exactly_the_marked_shards(budget):
+    """A broom (8 paths of 2,000 vertices hanging off vertex 0) in 256
+    shards: 8 vertices change per step, so every step after the first few is
+    selective, and each one sweeps exactly the shards that hold the last
+    step's changed vertices' out-neighbours (the partition activation of
+    GraphMP/system/GraphPS.h:349-368, exact per shard).  Resident graphs mark
+    them on the device from the out-edge CSR; streamed graphs list the changed
+    vertices for the host.  Values and per-step counts stay the reference's."""
+    k, L = 8, 2000
+    src, dst = [], []
+    for j in range(k):
+        head = 1 + j * L
+        src += [0] + list(range(head, head + L - 1))
+        dst += [head] + list(range(head + 1, head + L))
+    V = 1 + k * L
+    off, col = gx.build_csc(V, np.array(src, np.int32), np.array(dst, np.int32))
+    g = gx.Graph(V, off, col, None, 256)
+    ref, ch, _ = O.run(O.SSSP, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 5000, source=0)
+    cfg = {"push_sparse": 0}
+    if budget == "stream":
+        cfg.update(cache_budget_bytes=g.E * 4 // 3, stream_slots=2)
+    with engine_for(g, **cfg) as e:
+        st = e.run(gx.APP_SSSP, 5000, source=0)
+        assert np.array_equal(e.values(), ref)
+        assert np.array_equal(run_changed(e, st["iterations"]), ch)
+        stats = [e.iter_stats(i) for i in range(st["iterations"])]
+    checked = 0
+    for t, m in enumerate(stats):
+        if m["mode"] != 1 or m["shards_active"] == g.P or t < 2:
+            continue
+        assert m["shards_active"] == len(_frontier_shards(g, ref, t)), t
+        checked += 1
+    assert checked > L // 2
 
 
 @pytest.mark.parametrize("budget", [-1, 0])
