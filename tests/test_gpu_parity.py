@@ -371,10 +371,14 @@ def test_selective_steps_skip_shards_and_keep_values():
     st = e.run(gx.APP_SSSP, 5000, source=0)
     assert np.array_equal(e.values(), ref)
     assert np.array_equal(run_changed(e, st["iterations"]), ch)
-    sel = [e.iter_stats(i) for i in range(st["iterations"]) if e.iter_stats(i)["mode"] == 1]
-    assert len(sel) > V // 2
-    assert all(m["shards_active"] == 1 for m in sel[16:])
+    stats = [e.iter_stats(i) for i in range(st["iterations"])]
     e.close()
+    sel = [(t, m) for t, m in enumerate(stats) if m["mode"] == 1]
+    assert len(sel) > V // 2
+    # one shard per step (none after the last vertex, which has no out-edge)
+    for t, m in sel[16:]:
+        assert m["shards_active"] == len(_frontier_shards(g, ref, t)) <= 1, t
+    assert sum(m["shards_active"] == 1 for _, m in sel) > V // 2
 
 
 def _frontier_shards(g, dist, t):
