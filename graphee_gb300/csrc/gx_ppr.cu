@@ -15,9 +15,9 @@
 // and the call returns GX_ERR_TIMEOUT), and go on to the next step.  A unit
 // is one destination vertex, or a chunk of kPprChunk in-edges of a vertex
 // with more; its row is summed by a group of W/2 lanes (a float2 each), so a
-// warp works on 64/W units at once.  Chunked vertices fold their partial rows
-// in chunk order in the warp group that finishes last, so results are
-// deterministic.
+// warp works on 64/W units at once, from claims of kPprClaim units.  Chunked
+// vertices fold their partial rows in chunk order in the warp group that
+// finishes last, so results are deterministic.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -93,6 +93,10 @@ __device__ __forceinline__ void ppr_finish(const PprArgs& a, float* rs_out, floa
   *reinterpret_cast<float2*>(rs_out + row) = make_float2(r.x * inv, r.y * inv);
 }
 
+// Units a warp claims per cursor atomic: most vertices of an R-MAT graph
+// have no in-edges, so a claim per unit would cost a round trip per empty row.
+constexpr int kPprClaim = 16;
+
 template <int W>
 __global__ void __launch_bounds__(kPprThreads) ppr_kernel(const PprArgs a) {
   constexpr int L = W / 2;   // lanes per row, a float2 each
@@ -112,15 +116,15 @@ __global__ void __launch_bounds__(kPprThreads) ppr_kernel(const PprArgs a) {
       const int qb = static_cast<int>((static_cast<int64_t>(U) * q) / nq);
       const int qe = static_cast<int>((static_cast<int64_t>(U) * (q + 1)) / nq);
       int u0 = 0;
-      if (lane == 0) u0 = qb + static_cast<int>(atomicAdd(ctr + q, static_cast<unsigned>(G)));
+      if (lane == 0) u0 = qb + static_cast<int>(atomicAdd(ctr + q, static_cast<unsigned>(kPprClaim)));
       u0 = __shfl_sync(0xffffffffu, u0, 0);
       if (u0 >= qe) {
         q = next_queue(ctr, q, nq, U, lane);
         if (q < 0) break;
         continue;
       }
-      const int u = u0 + grp;
-      if (u < qe) {
+      // Group grp takes units u0 + grp, u0 + grp + G, ... of the claim.
+      for (int u = u0 + grp; u < u0 + kPprClaim && u < qe; u += G) {
         const int4 un = a.units[u];
         const int v = un.x;
         const int64_t vb = a.off[v], ve = a.off[v + 1];
