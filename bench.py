@@ -520,9 +520,29 @@ def run_cc_tc(args):
           tc_work_edges=st["edges_scanned"])
 
 
+def pinned_h2d_gbs(nbytes=2 << 30, repeats=7):
+    """The host link's rate for the streaming ring's kind of copy: one
+    cudaMemcpyAsync of pinned host memory to the device (torch's copy_ of a
+    pinned tensor), timed with CUDA events; the median of the repeats."""
+    import torch
+    h = torch.empty(nbytes, dtype=torch.uint8).pin_memory()
+    d = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    rates = []
+    for i in range(repeats + 1):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        d.copy_(h, non_blocking=True)
+        e1.record()
+        e1.synchronize()
+        if i:
+            rates.append(nbytes / (e0.elapsed_time(e1) / 1000) / 1e9)
+    del h, d
+    return statistics.median(rates)
+
+
 def run_stream(args):
     import graphee_gb300 as gx
-    scale = args.scale if args.scale != 24 else 28
+    scale = args.scale if args.scale not in (24, 26) else 28
     t0 = time.time()
     g = gx.rmat_graph(scale, args.edge_factor, seed=SEED, P=256, gpu=True)
     build_s = time.time() - t0
@@ -540,13 +560,22 @@ def run_stream(args):
     e.set_weights(w)
     del w
     ss = e.run(gx.APP_SSSP, 10000, source=0, weighted=True)
+    ss_steps = [e.iter_stats(i) for i in range(ss["iterations"])]
+    e.close()
+    link = pinned_h2d_gbs()
+    pr_gbs = pr["h2d_bytes"] / (pr["ms_copy"] / 1000) / 1e9 if pr["ms_copy"] > 0 else None
     _line("pagerank_gteps_streamed", 10 * g.E / (pr["ms_total"] / 1000) / 1e9, "GTEPS", args, cfg, dtype="f32",
           ms_per_superstep=pr["ms_total"] / 10, shards_resident=pr["shards_resident"],
           h2d_gb_per_superstep=pr["h2d_bytes"] / 10 / 1e9, copy_ms=pr["ms_copy"], compute_ms=pr["ms_compute"],
           overlap=pr["overlap"],
+          roofline={"bound": "host link", "achieved": pr_gbs, "peak": link, "unit": "GB/s",
+                    "frac": pr_gbs / link if pr_gbs else None,
+                    "peak_source": "measured here: pinned host-to-device cudaMemcpyAsync of 2 GiB, median of 7"},
+          link_frac=pr_gbs / link if pr_gbs else None,
           sssp={"gteps": g.E / (ss["ms_total"] / 1000) / 1e9, "ms": ss["ms_total"], "supersteps": ss["iterations"],
-                "h2d_gb": ss["h2d_bytes"] / 1e9, "overlap": ss["overlap"], "shards_streamed": ss["shards_streamed"]})
-    e.close()
+                "h2d_gb": ss["h2d_bytes"] / 1e9, "overlap": ss["overlap"], "shard_visits_streamed": ss["shards_streamed"],
+                "shards_swept_per_step": [s["shards_active"] for s in ss_steps],
+                "modes": [s["mode"] for s in ss_steps]})
 
 
 def run_batch(args):

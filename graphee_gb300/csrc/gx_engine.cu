@@ -421,8 +421,8 @@ gx_status plan_shards(gx_engine* e, const int32_t* src_col, bool col_on_device) 
 // Streamed graphs: for every vertex, the set of shards it is a source in
 // (a bitset of P bits), kept in host memory, where the host-driven step loop
 // turns the changed vertices a finalize lists into the shards the next
-// selective step streams and sweeps.  Built once, on the GPU, shard by shard
-// (streamed shards go through slot 0), then copied to the host.
+// selective step streams and sweeps.  Built at load, on the GPU, shard by
+// shard (streamed shards go through slot 0), then copied to the host.
 __global__ void shard_sets_kernel(unsigned long long* sets, int words, const int32_t* col, int64_t e0, int64_t e1,
                                   int32_t p) {
   const int w = p >> 6;
@@ -1304,7 +1304,9 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   if (!e->all_resident) {
     e->changed_cap = std::max<int64_t>(4096, V / 256);
     GX_TRY(dev_alloc(&e->d_changed_list, static_cast<size_t>(e->changed_cap)));
+    GX_TRY(build_shard_sets(e));
   }
+  phase("shard sets");
   if (e->all_resident) {
     if (e->h_col) cudaFreeHost(e->h_col);
     e->h_col = nullptr;
@@ -1366,6 +1368,7 @@ gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
         e->changed_cap = std::max<int64_t>(4096, e->V / 256);
         GX_TRY(dev_alloc(&e->d_changed_list, static_cast<size_t>(e->changed_cap)));
       }
+      if (!e->all_resident && e->shard_set_words == 0) GX_TRY(build_shard_sets(e));
       if (e->all_resident) {
         cudaFreeHost(e->h_col);
         e->h_col = nullptr;

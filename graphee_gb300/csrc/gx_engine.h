@@ -199,7 +199,7 @@ struct gx_engine {
   // Selective steps: shard bounds (P+1), two shard bitmaps marked by the
   // device (resident graphs), the changed-vertex list a streamed step hands
   // to the host and the host's per-vertex shard sets (P bits per vertex,
-  // built at a streamed graph's first selective step).
+  // built when a streamed graph is loaded).
   int32_t* d_bounds = nullptr;
   uint32_t* d_shard_bm = nullptr;
   int32_t* d_changed_list = nullptr;
