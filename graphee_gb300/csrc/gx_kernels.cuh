@@ -462,6 +462,50 @@ __device__ __forceinline__ typename AppTraits<APP>::T warp_reduce_range(const Pu
   return acc;
 }
 
+// Group-wise reduction of the edge range [b, e) by the 8 lanes of group
+// grp (lanes 8*grp .. 8*grp+7, all calling with the same range): each lane
+// takes 8 edges per round (two 128-bit index loads 32 edges apart), and the
+// lanes' partials meet in a fixed xor tree within the group.
+#ifndef GX_GROUP_SWEEP
+#define GX_GROUP_SWEEP 0
+#endif
+#ifndef GX_MID_MAX
+#define GX_MID_MAX 256
+#endif
+template <int APP, bool ASYNC = false, bool COMP = false, bool HOT = false>
+__device__ __forceinline__ typename AppTraits<APP>::T group_reduce_range(const PullArgs& a, const void* src_val,
+                                                                         const float* src_con, int64_t b, int64_t e,
+                                                                         int gl, int grp, const void* hot) {
+  typedef typename AppTraits<APP>::T T;
+  T acc = identity<APP>();
+  for (int64_t q = (b & ~3ll) + 4 * gl; q < e; q += 64) {
+    const int64_t q2 = q + 32;
+    const int4 c4 = load_idx4<COMP>(a, q);
+    int4 d4 = make_int4(0, 0, 0, 0);
+    if (q2 < e) d4 = load_idx4<COMP>(a, q2);
+    uint4 w4 = make_uint4(0, 0, 0, 0), x4 = make_uint4(0, 0, 0, 0);
+    if constexpr (APP == K_SSSP_W) {
+      w4 = load_w4<COMP>(a, q);
+      if (q2 < e) x4 = load_w4<COMP>(a, q2);
+    }
+    const int cs[8] = {c4.x, c4.y, c4.z, c4.w, d4.x, d4.y, d4.z, d4.w};
+    const uint32_t ws[8] = {w4.x, w4.y, w4.z, w4.w, x4.x, x4.y, x4.z, x4.w};
+    T vals[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int64_t k = (j < 4 ? q : q2) + (j & 3);
+      vals[j] = (k >= b && k < e) ? edge_value<APP, ASYNC, HOT>(a, src_val, src_con, cs[j], ws[j], hot)
+                                  : identity<APP>();
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc = combine<APP>(acc, vals[j]);
+  }
+  const unsigned gmask = 0xffu << (grp * 8);
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) acc = combine<APP>(acc, __shfl_xor_sync(gmask, acc, o));
+  return acc;
+}
+
 #ifndef GX_PULL_MIN_BLOCKS
 #define GX_PULL_MIN_BLOCKS 4
 #endif
@@ -729,8 +773,33 @@ __global__ void __launch_bounds__(pull_threads<HOT>(), HOT ? 1 : GX_PULL_MIN_BLO
               k = kn;
             }
           }
+          // Medium lists: four at a time, one per group of 8 lanes.
+          unsigned mbig = mlong;
+          if (GX_GROUP_SWEEP) {
+            unsigned mmid = __ballot_sync(0xffffffffu, longl && end - beg <= GX_MID_MAX);
+            mbig = mlong & ~mmid;
+            const int grp = lane >> 3, gl = lane & 7;
+            while (mmid) {
+              unsigned mm = mmid;  // group grp takes the grp-th lowest list left
+              for (int i = 0; i < grp; ++i) mm &= mm - 1;
+              const int l = mm ? __ffs(mm) - 1 : -1;
+#pragma unroll
+              for (int i = 0; i < 4; ++i) mmid &= mmid - 1;
+              const int sl = l < 0 ? 0 : l;
+              const int64_t bl = __shfl_sync(0xffffffffu, beg, sl);
+              const int64_t el = __shfl_sync(0xffffffffu, end, sl);
+              T r = identity<APP>();
+              if (l >= 0) r = group_reduce_range<APP, ASYNC, COMP, HOT>(a, src_val, src_con, bl, el, gl, grp, hot);
+#pragma unroll
+              for (int g = 0; g < 4; ++g) {
+                const int lg = __shfl_sync(0xffffffffu, l, 8 * g);
+                const T rg = __shfl_sync(0xffffffffu, r, 8 * g);
+                if (lane == lg) acc = combine<APP>(acc, rg);
+              }
+            }
+          }
           // Longer lists: the whole warp sweeps each one in turn.
-          for (unsigned m = mlong; m; m &= m - 1) {
+          for (unsigned m = mbig; m; m &= m - 1) {
             const int l = __ffs(m) - 1;
             const int64_t bl = __shfl_sync(0xffffffffu, beg, l);
             const int64_t el = __shfl_sync(0xffffffffu, end, l);
