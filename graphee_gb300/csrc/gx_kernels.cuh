@@ -462,24 +462,28 @@ __device__ __forceinline__ typename AppTraits<APP>::T warp_reduce_range(const Pu
   return acc;
 }
 
-// Group-wise reduction of the edge range [b, e) by the 8 lanes of group
-// grp (lanes 8*grp .. 8*grp+7, all calling with the same range): each lane
-// takes 8 edges per round (two 128-bit index loads 32 edges apart), and the
-// lanes' partials meet in a fixed xor tree within the group.
+// Group-wise reduction of the edge range [b, e) by the GL lanes of group
+// grp (lanes GL*grp .. GL*grp+GL-1, all calling with the same range): each
+// lane takes 8 edges per round (two 128-bit index loads 4*GL edges apart),
+// and the lanes' partials meet in a fixed xor tree within the group.
 #ifndef GX_GROUP_SWEEP
-#define GX_GROUP_SWEEP 0
+#define GX_GROUP_SWEEP 1
 #endif
 #ifndef GX_MID_MAX
-#define GX_MID_MAX 256
+#define GX_MID_MAX 128
 #endif
+#ifndef GX_GROUP_LANES
+#define GX_GROUP_LANES 8
+#endif
+constexpr int kGroupLanes = GX_GROUP_LANES;
 template <int APP, bool ASYNC = false, bool COMP = false, bool HOT = false>
 __device__ __forceinline__ typename AppTraits<APP>::T group_reduce_range(const PullArgs& a, const void* src_val,
                                                                          const float* src_con, int64_t b, int64_t e,
                                                                          int gl, int grp, const void* hot) {
   typedef typename AppTraits<APP>::T T;
   T acc = identity<APP>();
-  for (int64_t q = (b & ~3ll) + 4 * gl; q < e; q += 64) {
-    const int64_t q2 = q + 32;
+  for (int64_t q = (b & ~3ll) + 4 * gl; q < e; q += 8 * kGroupLanes) {
+    const int64_t q2 = q + 4 * kGroupLanes;
     const int4 c4 = load_idx4<COMP>(a, q);
     int4 d4 = make_int4(0, 0, 0, 0);
     if (q2 < e) d4 = load_idx4<COMP>(a, q2);
@@ -500,9 +504,9 @@ __device__ __forceinline__ typename AppTraits<APP>::T group_reduce_range(const P
 #pragma unroll
     for (int j = 0; j < 8; ++j) acc = combine<APP>(acc, vals[j]);
   }
-  const unsigned gmask = 0xffu << (grp * 8);
+  const unsigned gmask = kGroupLanes == 32 ? 0xffffffffu : (((1u << kGroupLanes) - 1u) << (grp * kGroupLanes));
 #pragma unroll
-  for (int o = 4; o > 0; o >>= 1) acc = combine<APP>(acc, __shfl_xor_sync(gmask, acc, o));
+  for (int o = kGroupLanes / 2; o > 0; o >>= 1) acc = combine<APP>(acc, __shfl_xor_sync(gmask, acc, o));
   return acc;
 }
 
@@ -773,27 +777,28 @@ __global__ void __launch_bounds__(pull_threads<HOT>(), HOT ? 1 : GX_PULL_MIN_BLO
               k = kn;
             }
           }
-          // Medium lists: four at a time, one per group of 8 lanes.
+          // Medium lists: several at a time, one per group of kGroupLanes lanes.
           unsigned mbig = mlong;
           if (GX_GROUP_SWEEP) {
+            constexpr int NG = 32 / kGroupLanes;
             unsigned mmid = __ballot_sync(0xffffffffu, longl && end - beg <= GX_MID_MAX);
             mbig = mlong & ~mmid;
-            const int grp = lane >> 3, gl = lane & 7;
+            const int grp = lane / kGroupLanes, gl = lane % kGroupLanes;
             while (mmid) {
               unsigned mm = mmid;  // group grp takes the grp-th lowest list left
               for (int i = 0; i < grp; ++i) mm &= mm - 1;
               const int l = mm ? __ffs(mm) - 1 : -1;
 #pragma unroll
-              for (int i = 0; i < 4; ++i) mmid &= mmid - 1;
+              for (int i = 0; i < NG; ++i) mmid &= mmid - 1;
               const int sl = l < 0 ? 0 : l;
               const int64_t bl = __shfl_sync(0xffffffffu, beg, sl);
               const int64_t el = __shfl_sync(0xffffffffu, end, sl);
               T r = identity<APP>();
               if (l >= 0) r = group_reduce_range<APP, ASYNC, COMP, HOT>(a, src_val, src_con, bl, el, gl, grp, hot);
 #pragma unroll
-              for (int g = 0; g < 4; ++g) {
-                const int lg = __shfl_sync(0xffffffffu, l, 8 * g);
-                const T rg = __shfl_sync(0xffffffffu, r, 8 * g);
+              for (int g = 0; g < NG; ++g) {
+                const int lg = __shfl_sync(0xffffffffu, l, kGroupLanes * g);
+                const T rg = __shfl_sync(0xffffffffu, r, kGroupLanes * g);
                 if (lane == lg) acc = combine<APP>(acc, rg);
               }
             }
