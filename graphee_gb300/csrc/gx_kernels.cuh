@@ -286,8 +286,9 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long x) {
 //    with in-degree <= kLaneMaxDegree walk their own edge list (two 128-bit
 //    index loads per step, next pair prefetched) and fold in edge order,
 //    which is the reference's summation order (pagerank.cpp:44-47); lanes
-//    with more edges are then swept by the whole warp one by one (coalesced
-//    index loads, a fixed-shape tree sum);
+//    with up to GX_MID_MAX edges are then swept four lists at a time by
+//    groups of 8 lanes, and longer lists by the whole warp one by one
+//    (coalesced index loads, fixed-shape tree sums);
 //  * a heavy vertex (in-degree > heavy) is split into chunks of kHeavyChunk
 //    edges; each chunk is reduced by one warp, and the warp that finishes a
 //    vertex's last chunk folds the partials in chunk order and applies it.
@@ -298,7 +299,7 @@ __device__ __forceinline__ unsigned long long warp_sum(unsigned long long x) {
 // ---------------------------------------------------------------------------
 constexpr int kHeavyChunk = 2048;
 #ifndef GX_LANE_MAX
-#define GX_LANE_MAX 32
+#define GX_LANE_MAX 16
 #endif
 #ifndef GX_GRAB
 #define GX_GRAB 4
