@@ -92,6 +92,25 @@ def build_apps() -> Path:
     return APP
 
 
+EXAMPLE = PKG / "libgx_program_example.so"
+
+
+def build_program_example() -> Path:
+    """Vertex programs plugged in from outside the library
+    (apps/gx_program_example.cu over include/gx_program.cuh), compiled like an
+    application would compile its own: nvcc against the headers and libgx.so."""
+    src = PKG / "apps" / "gx_program_example.cu"
+    deps = [src, LIB, ROOT / "include" / "gx_program.cuh", ROOT / "include" / "gx.h"]
+    if EXAMPLE.exists() and EXAMPLE.stat().st_mtime >= max(d.stat().st_mtime for d in deps):
+        return EXAMPLE
+    cmd = [NVCC] + ARCH + ["-O3", "-std=c++17", "-shared", "-Xcompiler", "-fPIC", "-I", str(ROOT / "include"),
+                           str(src), "-o", str(EXAMPLE), "-L", str(PKG), "-lgx", "-Xlinker", "-rpath,$ORIGIN"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"program example build failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")
+    return EXAMPLE
+
+
 # Where the build looks for the reference tree (read only, to compile the
 # reference's own apps as the oracle's pin); GX_REFERENCE_ROOT overrides it.
 REFERENCE_MOUNT = "/root/reference"
@@ -114,6 +133,7 @@ def build_oracle() -> None:
 def build(force: bool = False) -> None:
     build_lib(force)
     build_apps()
+    build_program_example()
     build_oracle()
 
 

@@ -1460,6 +1460,22 @@ gx_status gx_write_values_npy(gx_engine* e, const char* path) {
   return GX_OK;
 }
 
+gx_status gx_get_device_graph(gx_engine* e, gx_device_graph* out) {
+  if (!e || !out) return fail(GX_ERR_INVALID, "gx_get_device_graph: bad arguments");
+  if (!e->loaded) return fail(GX_ERR_STATE, "gx_get_device_graph: no graph loaded");
+  if (!e->all_resident) return fail(GX_ERR_STATE, "gx_get_device_graph: some shards are not resident");
+  out->V = e->V;
+  out->P = e->P;
+  out->E = e->E;
+  out->off = e->d_off;
+  out->col = e->d_col;
+  out->w = e->has_weights ? e->d_w : nullptr;
+  out->outdeg = e->d_outdeg;
+  out->bounds = e->d_bounds;
+  out->stream = e->s_comp;
+  return GX_OK;
+}
+
 gx_status gx_get_iter_stats(gx_engine* e, int32_t step, gx_iter_stats* out) {
   if (!e || !out) return fail(GX_ERR_INVALID, "gx_get_iter_stats: bad arguments");
   if (step < 0 || step >= e->last_steps)

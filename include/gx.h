@@ -192,6 +192,25 @@ gx_status gx_get_values(gx_engine* e, void* host_out);
 gx_status gx_write_values_npy(gx_engine* e, const char* path);
 gx_status gx_read_values_npy(const char* path, int64_t n, void* out);
 
+/* The engine's resident graph as device pointers, for vertex programs that
+ * run on it from the caller's own kernels (include/gx_program.cuh): the
+ * plug-in point that GraphPS<T>'s _comp function pointer and init_vertex()
+ * are in the reference (GraphMP/system/GraphPS.h:25-34,60).  Valid until the
+ * next load or gx_destroy; GX_ERR_STATE when some shard is not resident. */
+typedef struct gx_device_graph {
+  int32_t V;
+  int32_t P;
+  int64_t E;
+  const int64_t* off;      /* device: in-edge offsets, V+1 */
+  const int32_t* col;      /* device: source ids, E (+ 8 readable entries past the end) */
+  const uint32_t* w;       /* device: weights aligned with col, or NULL without gx_set_weights */
+  const int32_t* outdeg;   /* device: out-degree, V */
+  const int32_t* bounds;   /* device: shard bounds, P+1 */
+  void* stream;            /* cudaStream_t the engine computes on */
+} gx_device_graph;
+
+gx_status gx_get_device_graph(gx_engine* e, gx_device_graph* out);
+
 /* Per-step statistics of the last gx_run (the reference logs these per
  * iteration, GraphPS.h:375-382). */
 gx_status gx_get_iter_stats(gx_engine* e, int32_t step, gx_iter_stats* out);
