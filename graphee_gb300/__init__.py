@@ -45,7 +45,8 @@ class Config(C.Structure):
                 ("exact_order", C.c_int32),
                 ("push_sparse", C.c_int32), ("use_graph", C.c_int32), ("wait_limit", C.c_uint32),
                 ("verbose", C.c_int32), ("profile", C.c_int32),
-                ("compress_cache", C.c_int32), ("push_edge_fraction", C.c_double), ("hot_vertices", C.c_int32)]
+                ("compress_cache", C.c_int32), ("push_edge_fraction", C.c_double), ("hot_vertices", C.c_int32),
+                ("relabel", C.c_int32)]
 
 
 class RunParams(C.Structure):

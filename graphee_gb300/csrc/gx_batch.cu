@@ -481,6 +481,7 @@ gx_status gx_batch_run(gx_engine* e, int32_t n_inst, const int32_t* inst_vbegin,
   if (!e || n_inst < 1 || !inst_vbegin || pr_iters < 0 || cc_max_iter < 0)
     return fail(GX_ERR_INVALID, "gx_batch_run: bad arguments");
   if (!e->loaded || !e->all_resident) return fail(GX_ERR_STATE, "gx_batch_run: load the packed graph first (all resident)");
+  if (e->relabeled) return fail(GX_ERR_STATE, "gx_batch_run: the engine renumbered the vertices (config.relabel)");
   gx_batch_tuning t;
   gx_batch_tuning_default(&t);
   if (tuning) t = *tuning;
@@ -522,6 +523,7 @@ gx_status gx_batch_autotune(gx_engine* e, int32_t n_inst, const int32_t* inst_vb
   gx::NvtxRange nvtx_range("gx_batch_autotune");
   if (!e || !best || n_inst < 1 || !inst_vbegin) return fail(GX_ERR_INVALID, "gx_batch_autotune: bad arguments");
   if (!e->loaded || !e->all_resident) return fail(GX_ERR_STATE, "gx_batch_autotune: load the packed graph first");
+  if (e->relabeled) return fail(GX_ERR_STATE, "gx_batch_autotune: the engine renumbered the vertices (config.relabel)");
   GX_CUDA(cudaSetDevice(e->dev));
   BatchDev d;
   BatchArgs a;

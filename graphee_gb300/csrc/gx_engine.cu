@@ -174,6 +174,92 @@ void build_units(gx_engine* e) {
   e->n_partials = n_part[P];
 }
 
+// Longest in-list a warp rewrites when the engine relabels; longer ones go
+// to a CTA each.
+constexpr int64_t kRelabelWarpMax = 65536;
+
+// The relabelling order on the host: in each shard, the vertices by
+// descending in-degree (capped at 4095, stable in the caller's numbering), by
+// a counting sort per shard.  Fills h_inv / h_perm and turns e->off and
+// e->outdeg into the new numbering.
+void relabel_host(gx_engine* e) {
+  const int32_t V = e->V, P = e->P;
+  const int64_t* off = e->off.data();
+  e->h_inv.resize(static_cast<size_t>(V));
+  e->h_perm.resize(static_cast<size_t>(V));
+  int32_t* inv = e->h_inv.data();
+  int32_t* perm = e->h_perm.data();
+  constexpr int kKeys = 4096;
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int32_t p = 0; p < P; ++p) {
+    const int32_t b = e->bounds[p], t = e->bounds[p + 1];
+    std::vector<int32_t> start(kKeys + 1, 0);
+    auto key = [&](int32_t v) {  // descending in-degree: key 0 is the largest
+      const int64_t d = off[v + 1] - off[v];
+      return kKeys - 1 - static_cast<int>(d < kKeys - 1 ? d : kKeys - 1);
+    };
+    for (int32_t v = b; v < t; ++v) ++start[key(v) + 1];
+    for (int k = 0; k < kKeys; ++k) start[k + 1] += start[k];
+    for (int32_t v = b; v < t; ++v) inv[b + start[key(v)]++] = v;
+  }
+  hvec<int64_t> noff(static_cast<size_t>(V) + 1);
+  hvec<int32_t> nod(static_cast<size_t>(V));
+  std::vector<int64_t> part;
+#pragma omp parallel
+  {
+    const int nt = omp_get_num_threads(), t = omp_get_thread_num();
+#pragma omp single
+    part.assign(static_cast<size_t>(nt) + 1, 0);
+    const int64_t lo = static_cast<int64_t>(V) * t / nt, hi = static_cast<int64_t>(V) * (t + 1) / nt;
+    int64_t sum = 0;
+    for (int64_t i = lo; i < hi; ++i) {
+      const int32_t v = inv[i];
+      perm[v] = static_cast<int32_t>(i);
+      nod[i] = e->outdeg[v];
+      sum += off[v + 1] - off[v];
+    }
+    part[t + 1] = sum;
+#pragma omp barrier
+#pragma omp single
+    for (int i = 0; i < nt; ++i) part[i + 1] += part[i];
+    int64_t run = part[t];
+    for (int64_t i = lo; i < hi; ++i) {
+      noff[i] = run;
+      run += off[inv[i] + 1] - off[inv[i]];
+    }
+  }
+  noff[V] = off[V];
+  e->relabel_longs.clear();
+  for (int32_t i = 0; i < V; ++i)
+    if (noff[i + 1] - noff[i] > kRelabelWarpMax) e->relabel_longs.push_back(i);
+  e->off.swap(noff);
+  e->outdeg.swap(nod);
+}
+
+// Rewrites per-edge data laid out by the caller's offsets (d_off_old) into
+// the relabelled layout: source ids renamed through d_perm (perm = true), or
+// values copied (weights).
+gx_status relabel_device_lists(gx_engine* e, const int32_t* src, int32_t* dst, bool perm, cudaStream_t s) {
+  relabel_lists_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, src, e->d_off, e->d_inv, perm ? e->d_perm : nullptr,
+                                                   e->V, kRelabelWarpMax, dst);
+  GX_CUDA(cudaGetLastError());
+  if (!e->relabel_longs.empty()) {
+    relabel_long_kernel<<<static_cast<int>(e->relabel_longs.size()), 1024, 0, s>>>(
+        e->d_off_old, src, e->d_off, e->d_inv, perm ? e->d_perm : nullptr, e->d_longs, dst);
+    GX_CUDA(cudaGetLastError());
+  }
+  GX_CUDA(cudaStreamSynchronize(s));
+  return GX_OK;
+}
+
+// Values in the caller's numbering from the engine's buffer (d_stage).
+gx_status values_to_caller(gx_engine* e, const void* d_vals, cudaStream_t s) {
+  gather_values_kernel<<<e->n_sm * 4, 256, 0, s>>>(static_cast<const uint32_t*>(d_vals), e->d_perm, e->V, e->d_stage);
+  GX_CUDA(cudaGetLastError());
+  GX_CUDA(cudaStreamSynchronize(s));
+  return GX_OK;
+}
+
 gx_status alloc_ctl(gx_engine* e) {
   if (!e->d_ctl) GX_TRY(dev_alloc(&e->d_ctl, 1));
   if (!e->h_ctl) GX_CUDA(cudaHostAlloc(reinterpret_cast<void**>(&e->h_ctl), sizeof(Ctl), cudaHostAllocDefault));
@@ -564,15 +650,26 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
     use_init = 1;  // values already placed in d_val[0] on the device (warm start)
   } else if (prm.use_init) {
     if (!e->has_init) return fail(GX_ERR_STATE, "gx_run: use_init set but gx_set_init was not called");
-    GX_CUDA(cudaMemcpy(e->d_val[0], e->init_vals.data(), sizeof(T) * V, cudaMemcpyHostToDevice));
+    if (e->relabeled) {
+      // The caller's values, moved into the engine's numbering.
+      GX_CUDA(cudaMemcpy(e->d_stage, e->init_vals.data(), sizeof(T) * V, cudaMemcpyHostToDevice));
+      scatter_values_kernel<<<e->n_sm * 4, 256, 0, e->s_comp>>>(e->d_stage, e->d_perm, V,
+                                                                static_cast<uint32_t*>(e->d_val[0]));
+      GX_CUDA(cudaGetLastError());
+    } else {
+      GX_CUDA(cudaMemcpy(e->d_val[0], e->init_vals.data(), sizeof(T) * V, cudaMemcpyHostToDevice));
+    }
     use_init = 1;
   }
+  // The source in the engine's numbering.
+  const int32_t source = (e->relabeled && prm.source >= 0 && prm.source < V) ? e->h_perm[prm.source] : prm.source;
   if (APP == K_PR_STD) {
-    // D of the initial vector, in the same fixed point the device uses.
+    // D of the initial vector, in the same fixed point the device uses (summed
+    // in the caller's vertex order).
     double D = 0;
     if (use_init && !e->device_init) {
       for (int32_t v = 0; v < V; ++v) {
-        if (e->outdeg[v] != 0) continue;
+        if (e->outdeg[e->relabeled ? e->h_perm[v] : v] != 0) continue;
         float x;
         memcpy(&x, &e->init_vals[v], sizeof(float));
         D += x;
@@ -587,8 +684,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   std::vector<int4> src_entries;
   if (push_ok && (APP == K_SSSP_UNIT || APP == K_SSSP_W) && !use_init && c.push_edge_limit > 0 &&
       prm.max_iter > 0) {
-    const int32_t od = e->outdeg[prm.source];
-    for (int32_t k = 0; k < od; k += kPushChunk) src_entries.push_back(make_int4(prm.source, 0, k, 0));
+    const int32_t od = e->outdeg[source];
+    for (int32_t k = 0; k < od; k += kPushChunk) src_entries.push_back(make_int4(source, 0, k, 0));
     c.step0_push = 1;
     c.mode = MODE_PUSH;
     c.n_frontier = static_cast<int>(src_entries.size());
@@ -597,8 +694,8 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
                               cudaMemcpyHostToDevice, e->s_comp));
   }
   GX_CUDA(cudaMemcpyAsync(e->d_ctl, &c, sizeof(Ctl), cudaMemcpyHostToDevice, e->s_comp));
-  init_kernel<APP><<<e->n_sm * 4, 256, 0, e->s_comp>>>(e->d_ctl, e->d_val[0], e->d_con[0], e->d_outdeg, V,
-                                                       prm.source, use_init);
+  init_kernel<APP><<<e->n_sm * 4, 256, 0, e->s_comp>>>(e->d_ctl, e->d_val[0], e->d_con[0], e->d_outdeg, V, source,
+                                                       use_init, e->relabeled ? e->d_inv : nullptr);
   GX_CUDA(cudaGetLastError());
   GX_CUDA(cudaMemsetAsync(e->d_bm, 0, sizeof(uint32_t) * e->n_words, e->s_comp));
   GX_CUDA(cudaMemsetAsync(e->d_work, 0, sizeof(unsigned int) * e->n_work, e->s_comp));
@@ -702,8 +799,12 @@ gx_status run_app(gx_engine* e, const gx_run_params& prm, gx_run_stats* out) {
   auto checkpoint = [&](const Ctl& hc) -> gx_status {
     if (!every || hc.step == last_ckpt || hc.step % every != 0) return GX_OK;
     ckpt_buf.resize(static_cast<size_t>(V));
-    GX_CUDA(cudaMemcpy(ckpt_buf.data(), hc.cur ? e->d_val[1] : e->d_val[0], sizeof(uint32_t) * V,
-                       cudaMemcpyDeviceToHost));
+    const void* cur_vals = hc.cur ? e->d_val[1] : e->d_val[0];
+    if (e->relabeled) {
+      GX_TRY(values_to_caller(e, cur_vals, e->s_comp));
+      cur_vals = e->d_stage;
+    }
+    GX_CUDA(cudaMemcpy(ckpt_buf.data(), cur_vals, sizeof(uint32_t) * V, cudaMemcpyDeviceToHost));
     const std::string path = std::string(prm.checkpoint_prefix) + std::to_string(hc.step) + ".npy";
     const char* descr = is_pr<APP>() ? "<f4" : (APP == K_SSSP_W ? "<u4" : "<i4");
     if (!write_npy_4(path, ckpt_buf.data(), V, descr)) return fail(GX_ERR_IO, "cannot write checkpoint %s", path.c_str());
@@ -1044,6 +1145,7 @@ void gx_config_default(gx_config* cfg) {
   cfg->push_edge_fraction = 0.5;
   cfg->compress_cache = 1;
   cfg->hot_vertices = 0;
+  cfg->relabel = 0;
 }
 
 void gx_run_params_default(gx_run_params* p, gx_app app) {
@@ -1153,28 +1255,42 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   // stream, while the host prepares the work units below.
   const bool direct = e->cfg.cache_budget_bytes < 0;
   // Small device buffers of the load; freed once the copy stream is idle.
+  // Relabelling (config.relabel): the caller's offsets and ids go to the
+  // device as they are, are checked there, and are rewritten into the new
+  // numbering once the host has computed it.
+  const bool relabel = direct && e->cfg.relabel != 0;
   struct Scratch {
     cudaStream_t s;
     unsigned int* flag = nullptr;
+    int32_t* col_old = nullptr;
     ~Scratch() {
-      if (flag) cudaStreamSynchronize(s);
+      if (flag || col_old) cudaStreamSynchronize(s);
       dev_free(&flag);
+      dev_free(&col_old);
     }
   } scratch{e->s_copy};
   if (direct) {
     GX_TRY(dev_alloc(&e->d_off, static_cast<size_t>(V) + 1));
     GX_TRY(dev_alloc(&e->d_col, static_cast<size_t>(E) + 8));
     GX_CUDA(cudaMemsetAsync(e->d_col + E, 0, 8 * sizeof(int32_t), e->s_copy));
-    GX_TRY(upload_async(e, e->d_off, off, sizeof(int64_t) * (static_cast<size_t>(V) + 1), e->s_copy));
-    GX_TRY(upload_async(e, e->d_col, col, sizeof(int32_t) * static_cast<size_t>(E), e->s_copy));
-    if (outdeg) {
+    int64_t* up_off = e->d_off;
+    int32_t* up_col = e->d_col;
+    if (relabel) {
+      GX_TRY(dev_alloc(&e->d_off_old, static_cast<size_t>(V) + 1));
+      GX_TRY(dev_alloc(&scratch.col_old, static_cast<size_t>(E) + 8));
+      up_off = e->d_off_old;
+      up_col = scratch.col_old;
+    }
+    GX_TRY(upload_async(e, up_off, off, sizeof(int64_t) * (static_cast<size_t>(V) + 1), e->s_copy));
+    GX_TRY(upload_async(e, up_col, col, sizeof(int32_t) * static_cast<size_t>(E), e->s_copy));
+    if (outdeg && !relabel) {
       GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
       GX_TRY(upload_async(e, e->d_outdeg, outdeg, sizeof(int32_t) * static_cast<size_t>(V), e->s_copy));
     }
     // Behind the uploads: the load-time checks.
     GX_TRY(dev_alloc(&scratch.flag, 1));
     GX_CUDA(cudaMemsetAsync(scratch.flag, 0, sizeof(unsigned int), e->s_copy));
-    validate_csc_kernel<<<e->n_sm * 8, 256, 0, e->s_copy>>>(e->d_off, V, e->d_col, E, scratch.flag);
+    validate_csc_kernel<<<e->n_sm * 8, 256, 0, e->s_copy>>>(up_off, V, up_col, E, scratch.flag);
     GX_CUDA(cudaGetLastError());
   }
   e->bounds.assign(bounds, bounds + P + 1);
@@ -1195,6 +1311,20 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
 #pragma omp parallel for reduction(+ : n_dang)
   for (int32_t v = 0; v < V; ++v) n_dang += e->outdeg[v] == 0;
   e->n_dangling = n_dang;
+  if (relabel) {
+    relabel_host(e);
+    phase("relabelled");
+    GX_TRY(upload_async(e, e->d_off, e->off.data(), sizeof(int64_t) * (static_cast<size_t>(V) + 1), e->s_copy));
+    GX_TRY(dev_alloc(&e->d_perm, static_cast<size_t>(V)));
+    GX_TRY(dev_alloc(&e->d_inv, static_cast<size_t>(V)));
+    GX_TRY(dev_alloc(&e->d_longs, std::max<size_t>(e->relabel_longs.size(), 1)));
+    GX_TRY(dev_alloc(&e->d_stage, static_cast<size_t>(V)));
+    GX_TRY(upload_async(e, e->d_perm, e->h_perm.data(), sizeof(int32_t) * static_cast<size_t>(V), e->s_copy));
+    GX_TRY(upload_async(e, e->d_inv, e->h_inv.data(), sizeof(int32_t) * static_cast<size_t>(V), e->s_copy));
+    if (!e->relabel_longs.empty())
+      GX_CUDA(cudaMemcpyAsync(e->d_longs, e->relabel_longs.data(), sizeof(int32_t) * e->relabel_longs.size(),
+                              cudaMemcpyHostToDevice, e->s_copy));
+  }
   // With a shard-cache budget not every shard reaches the device: check the
   // source ids on the host.  Otherwise the device checks them after the
   // upload, before any kernel indexes with them.
@@ -1226,7 +1356,7 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
     GX_TRY(dev_alloc(&e->d_off, static_cast<size_t>(V) + 1));
     GX_CUDA(cudaMemcpy(e->d_off, off, sizeof(int64_t) * (V + 1), cudaMemcpyHostToDevice));
   }
-  if (!(direct && outdeg)) {
+  if (!(direct && outdeg) || relabel) {
     GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
     GX_CUDA(cudaMemcpy(e->d_outdeg, e->outdeg.data(), sizeof(int32_t) * V, cudaMemcpyHostToDevice));
   }
@@ -1270,6 +1400,12 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
     if (h & 2u) {
       e->release_graph();
       return fail(GX_ERR_INVALID, "gx_load_csc: source id outside [0, %d)", V);
+    }
+    if (relabel) {
+      // The ids are in range: rename them into the new numbering.
+      GX_TRY(relabel_device_lists(e, scratch.col_old, e->d_col, true, e->s_copy));
+      e->relabeled = true;
+      phase("rewritten");
     }
   }
   GX_TRY(plan_shards(e, src_col, direct));
@@ -1334,11 +1470,23 @@ gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
   GX_CUDA(cudaSetDevice(e->dev));
   if (!e->all_resident && !e->h_col) return fail(GX_ERR_STATE, "gx_set_weights: streaming source missing");
   if (e->all_resident && e->cfg.cache_budget_bytes < 0) {
-    // No budget: the weights go straight to the device.
+    // No budget: the weights go straight to the device (a relabelled engine
+    // moves them into its own layout there).
     e->has_weights = true;
     GX_TRY(dev_alloc(&e->d_w, static_cast<size_t>(e->E) + 8));
     GX_CUDA(cudaMemsetAsync(e->d_w + e->E, 0, 8 * sizeof(uint32_t), e->s_copy));
-    GX_TRY(upload_async(e, e->d_w, w, sizeof(uint32_t) * static_cast<size_t>(e->E), e->s_copy));
+    if (e->relabeled) {
+      uint32_t* w_old = nullptr;
+      GX_TRY(dev_alloc(&w_old, static_cast<size_t>(e->E) + 1));
+      gx_status st = upload_async(e, w_old, w, sizeof(uint32_t) * static_cast<size_t>(e->E), e->s_copy);
+      if (st == GX_OK)
+        st = relabel_device_lists(e, reinterpret_cast<const int32_t*>(w_old), reinterpret_cast<int32_t*>(e->d_w),
+                                  false, e->s_copy);
+      gx::pool_free(w_old);
+      GX_TRY(st);
+    } else {
+      GX_TRY(upload_async(e, e->d_w, w, sizeof(uint32_t) * static_cast<size_t>(e->E), e->s_copy));
+    }
     GX_CUDA(cudaStreamSynchronize(e->s_copy));
     e->out_built = false;
     return GX_OK;
@@ -1444,7 +1592,12 @@ gx_status gx_get_values(gx_engine* e, void* host_out) {
   GX_CUDA(cudaSetDevice(e->dev));
   GX_CUDA(cudaMemcpy(e->h_ctl, e->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost));
   const int cur = e->h_ctl->cur & 1;
-  GX_CUDA(cudaMemcpy(host_out, e->d_val[cur], sizeof(uint32_t) * e->V, cudaMemcpyDeviceToHost));
+  const void* src = e->d_val[cur];
+  if (e->relabeled) {
+    GX_TRY(values_to_caller(e, src, e->s_comp));
+    src = e->d_stage;
+  }
+  GX_CUDA(cudaMemcpy(host_out, src, sizeof(uint32_t) * e->V, cudaMemcpyDeviceToHost));
   return GX_OK;
 }
 
@@ -1464,6 +1617,9 @@ gx_status gx_get_device_graph(gx_engine* e, gx_device_graph* out) {
   if (!e || !out) return fail(GX_ERR_INVALID, "gx_get_device_graph: bad arguments");
   if (!e->loaded) return fail(GX_ERR_STATE, "gx_get_device_graph: no graph loaded");
   if (!e->all_resident) return fail(GX_ERR_STATE, "gx_get_device_graph: some shards are not resident");
+  if (e->relabeled)
+    return fail(GX_ERR_STATE, "gx_get_device_graph: the engine renumbered the vertices (config.relabel); load "
+                              "without it");
   out->V = e->V;
   out->P = e->P;
   out->E = e->E;

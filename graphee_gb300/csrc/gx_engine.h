@@ -220,6 +220,18 @@ struct gx_engine {
   unsigned int* d_work = nullptr;
   int32_t n_work = 0;
 
+  // Relabelled engine (config.relabel): new vertex i is the caller's vertex
+  // h_inv[i], and h_perm maps back.  d_off_old keeps the caller's offsets for
+  // gx_set_weights; d_stage carries values between the two numberings;
+  // relabel_longs lists the new vertices whose in-lists a CTA rewrites.
+  bool relabeled = false;
+  std::vector<int32_t> h_perm, h_inv, relabel_longs;
+  int32_t* d_perm = nullptr;
+  int32_t* d_inv = nullptr;
+  int32_t* d_longs = nullptr;
+  int64_t* d_off_old = nullptr;
+  uint32_t* d_stage = nullptr;
+
   std::vector<uint32_t> init_vals;
   bool has_init = false;
   bool device_init = false;          // next gx_run starts from d_val[0] as it is
@@ -270,6 +282,15 @@ struct gx_engine {
     gx::dev_free(&d_partial);
     gx::dev_free(&d_hticket);
     gx::dev_free(&d_bm);
+    gx::dev_free(&d_perm);
+    gx::dev_free(&d_inv);
+    gx::dev_free(&d_longs);
+    gx::dev_free(&d_off_old);
+    gx::dev_free(&d_stage);
+    relabeled = false;
+    h_perm.clear();
+    h_inv.clear();
+    relabel_longs.clear();
     gx::dev_free(&d_bounds);
     gx::dev_free(&d_shard_bm);
     gx::dev_free(&d_changed_list);

@@ -1075,8 +1075,11 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
 }
 
 // Initial values (init_vertex of each app) and PageRank contributions.
+// label (nullable): CC's start label of each vertex, its id as the caller
+// numbered it (a relabelled engine), else the vertex's own index.
 template <int APP>
-__global__ void init_kernel(Ctl* ctl, void* val, float* con, const int32_t* outdeg, int n, int source, int use_init) {
+__global__ void init_kernel(Ctl* ctl, void* val, float* con, const int32_t* outdeg, int n, int source, int use_init,
+                            const int32_t* label = nullptr) {
   typedef typename AppTraits<APP>::T T;
   T* v = static_cast<T*>(val);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -1084,7 +1087,7 @@ __global__ void init_kernel(Ctl* ctl, void* val, float* con, const int32_t* outd
       if constexpr (is_pr<APP>()) v[i] = static_cast<float>(ctl->inv_n);  // assign(V, 1.0/V), pagerank.cpp:81
       else if constexpr (APP == K_SSSP_UNIT) v[i] = i == source ? 0 : kGpsInf;  // sssp.cpp:70-72
       else if constexpr (APP == K_SSSP_W) v[i] = i == source ? 0u : kInfW;
-      else if constexpr (APP == K_CC) v[i] = i;  // cc.cpp:70-73
+      else if constexpr (APP == K_CC) v[i] = label ? label[i] : i;  // cc.cpp:70-73
       else v[i] = 0;  // cal.cpp:77
     }
     if constexpr (is_pr<APP>()) {
@@ -1105,6 +1108,38 @@ static __global__ void validate_csc_kernel(const int64_t* off, int32_t V, const 
   if (col)
     for (int64_t k = tid; k < E; k += nt) f |= (col[k] < 0 || col[k] >= V) ? 2u : 0u;
   if (f) atomicOr(flag, f);
+}
+
+// Relabelling: new vertex i is old vertex inv[i].  Its in-list is the old
+// one, in the same order, with every source renamed through perm (perm null:
+// the entries are copied as they are, for weights).  A warp per list, for
+// lists of at most max_len; rel_long_kernel takes the longer ones, a CTA each.
+static __global__ void relabel_lists_kernel(const int64_t* off_old, const int32_t* src, const int64_t* off_new,
+                                            const int32_t* inv, const int32_t* perm, int32_t V, int64_t max_len,
+                                            int32_t* dst) {
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < V; i += warps) {
+    const int32_t v = inv[i];
+    const int64_t b0 = off_old[v], n = off_old[v + 1] - b0, b1 = off_new[i];
+    if (n > max_len) continue;
+    for (int64_t j = lane; j < n; j += 32) dst[b1 + j] = perm ? perm[src[b0 + j]] : src[b0 + j];
+  }
+}
+static __global__ void relabel_long_kernel(const int64_t* off_old, const int32_t* src, const int64_t* off_new,
+                                           const int32_t* inv, const int32_t* perm, const int32_t* longs,
+                                           int32_t* dst) {
+  const int32_t i = longs[blockIdx.x];
+  const int32_t v = inv[i];
+  const int64_t b0 = off_old[v], n = off_old[v + 1] - b0, b1 = off_new[i];
+  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) dst[b1 + j] = perm ? perm[src[b0 + j]] : src[b0 + j];
+}
+// out[v] = in[perm[v]] (values to the caller's numbering), and the inverse.
+static __global__ void gather_values_kernel(const uint32_t* in, const int32_t* perm, int32_t V, uint32_t* out) {
+  for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) out[v] = in[perm[v]];
+}
+static __global__ void scatter_values_kernel(const uint32_t* in, const int32_t* perm, int32_t V, uint32_t* out) {
+  for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) out[perm[v]] = in[v];
 }
 
 // Out-edge CSR from the CSC (counting sort by source; order within a source

@@ -1000,7 +1000,16 @@ gx_status gx_mlp_predict(gx_mlp* m, gx_engine* e, double damping, float* host_ou
   if (ms_mlp) *ms_mlp = t1;
   e->device_init_dangling = D / S;
   e->last_uniform_resid = ures;
-  if (host_out) GX_CUDA(cudaMemcpy(host_out, dst, sizeof(float) * V, cudaMemcpyDeviceToHost));
+  if (host_out) {
+    const void* src = dst;
+    if (e->relabeled) {  // back to the caller's numbering
+      gather_values_kernel<<<grid, 256, 0, s>>>(reinterpret_cast<const uint32_t*>(dst), e->d_perm, V, e->d_stage);
+      GX_CUDA(cudaGetLastError());
+      src = e->d_stage;
+    }
+    GX_CUDA(cudaMemcpyAsync(host_out, src, sizeof(float) * V, cudaMemcpyDeviceToHost, s));
+    GX_CUDA(cudaStreamSynchronize(s));
+  }
   return GX_OK;
 }
 

@@ -21,6 +21,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstring>
 #include <vector>
 
 #include "gx_engine.h"
@@ -258,7 +259,7 @@ extern "C" gx_status gx_ppr(gx_engine* e, int32_t k, const int32_t* sources, int
   guard.p.push_back(abort_flag);
 
   int32_t h_src[kPprMaxCols];
-  for (int j = 0; j < kPprMaxCols; ++j) h_src[j] = j < k ? sources[j] : -1;
+  for (int j = 0; j < kPprMaxCols; ++j) h_src[j] = j < k ? (e->relabeled ? e->h_perm[sources[j]] : sources[j]) : -1;
   GX_CUDA(cudaMemcpyAsync(d_units, units.data(), sizeof(int4) * units.size(), cudaMemcpyHostToDevice, s));
   GX_CUDA(cudaMemcpyAsync(d_src, h_src, sizeof(h_src), cudaMemcpyHostToDevice, s));
   GX_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned int) * std::max(n_part, 1), s));
@@ -343,9 +344,19 @@ extern "C" gx_status gx_ppr(gx_engine* e, int32_t k, const int32_t* sources, int
     if (iters == 0) {
       memset(host_out, 0, sizeof(float) * static_cast<size_t>(V) * k);
       for (int j = 0; j < k; ++j) host_out[static_cast<size_t>(sources[j]) * k + j] = 1.f;
-    } else {
+    } else if (!e->relabeled) {
       GX_CUDA(cudaMemcpy2D(host_out, sizeof(float) * k, r, sizeof(float) * W, sizeof(float) * k, V,
                            cudaMemcpyDeviceToHost));
+    } else {
+      // Rows in the engine's numbering: row v of the result is row perm[v].
+      std::vector<float> rows(static_cast<size_t>(V) * k);
+      GX_CUDA(cudaMemcpy2D(rows.data(), sizeof(float) * k, r, sizeof(float) * W, sizeof(float) * k, V,
+                           cudaMemcpyDeviceToHost));
+      const int32_t* perm = e->h_perm.data();
+#pragma omp parallel for schedule(static)
+      for (int32_t v = 0; v < V; ++v)
+        memcpy(host_out + static_cast<size_t>(v) * k, rows.data() + static_cast<size_t>(perm[v]) * k,
+               sizeof(float) * k);
     }
   }
   if (stats) {

@@ -90,6 +90,13 @@ typedef struct gx_config {
   int32_t hot_vertices;        /* resident pull steps: sources [0, hot_vertices) are gathered from a
                                   table in shared memory, filled at the start of each pull launch
                                   (capped by the shared memory of one CTA; 0 = off, the default) */
+  int32_t relabel;             /* 1: a load without a shard-cache budget renumbers the vertices of each
+                                  shard by descending in-degree (each in-list keeps its order), so the
+                                  pull kernel's tiles hold lists of like length and the hot sources
+                                  share cache lines.  Every call still speaks the caller's numbering
+                                  (values, start values, sources, CC labels, weights, checkpoints, PPR
+                                  rows); gx_batch_run and gx_get_device_graph refuse such an engine.
+                                  0 = off (the default) */
 } gx_config;
 
 typedef struct gx_run_params {
