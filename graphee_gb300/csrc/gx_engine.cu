@@ -195,7 +195,8 @@ void relabel_host(gx_engine* e) {
     const int32_t b = e->bounds[p], t = e->bounds[p + 1];
     std::vector<int32_t> start(kKeys + 1, 0);
     auto key = [&](int32_t v) {  // descending in-degree: key 0 is the largest
-      const int64_t d = off[v + 1] - off[v];
+      // (clamped at 0: the device has not yet checked that off is monotone)
+      const int64_t d = std::max<int64_t>(off[v + 1] - off[v], 0);
       return kKeys - 1 - static_cast<int>(d < kKeys - 1 ? d : kKeys - 1);
     };
     for (int32_t v = b; v < t; ++v) ++start[key(v) + 1];

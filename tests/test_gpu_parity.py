@@ -336,13 +336,13 @@ def test_cpp_app_drivers_vs_oracle(tmp_path):
     assert int(r.stdout.strip()) == O.triangles(s.V, s.off, s.col)
 
 
-@pytest.mark.parametrize("budget", [-1, 1 << 20])
-def test_load_rejects_bad_csc(budget):
+@pytest.mark.parametrize("budget,relabel", [(-1, 0), (1 << 20, 0), (-1, 1)])
+def test_load_rejects_bad_csc(budget, relabel):
     g = gx.rmat_graph(10, 8, seed=3, P=4)
     col = g.col.copy()
     col[17] = g.V + 5
     bad = gx.Graph(g.V, g.off, col, g.outdeg, g.P, g.bounds)
-    with gx.Engine(cache_budget_bytes=budget) as e:
+    with gx.Engine(cache_budget_bytes=budget, relabel=relabel) as e:
         with pytest.raises(gx.GxError) as ei:
             e.load(bad)
         assert ei.value.status == gx.GX_ERR_INVALID and "source id" in str(ei.value)
