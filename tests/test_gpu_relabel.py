@@ -3,7 +3,8 @@ vertices are renumbered by descending in-degree, each keeping its in-list in
 the caller's order with renamed sources.  Everything at the boundary stays in
 the caller's numbering, so every result must equal the plain engine's and the
 oracle's: PageRank bit-exact in exact-order mode with the per-step `Update`
-counts, the default mode within 1e-5 of the reference's ranks, SSSP (weighted
+counts, the default mode within 1e-5 of the reference's ranks and of the
+plain engine's, SSSP (weighted
 and unit) and CC values and counts bit-exact, start values, checkpoints and
 resumed runs, PPR rows, triangle counts and the warm-start predictions."""
 import ctypes as C
@@ -51,8 +52,10 @@ def test_pagerank_default_mode_matches_plain_engine(rmat16):
         e.run(gx.APP_PAGERANK_REF, 20)
         plain = e.values().copy()
     assert np.abs(got.astype(np.float64) - ref).max() / ref.max() < 1e-5
-    # Each vertex folds the same list in the same order either way.
-    assert np.array_equal(got.view(np.uint32), plain.view(np.uint32))
+    # The default mode tree-reduces a list in a shape that depends on where
+    # the list falls in its sweep, so the two layouts round differently (an
+    # ulp here and there), within the same bar.
+    assert (np.abs(got.astype(np.float64) - plain) / plain).max() < 1e-5
 
 
 def test_pagerank_std_matches_plain_engine(rmat16):
