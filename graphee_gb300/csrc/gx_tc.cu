@@ -55,13 +55,21 @@ __device__ __forceinline__ bool tc_before(int32_t du, int32_t u, int32_t dv, int
 // kernels' length).  Self-loops never qualify: u is not before itself.
 constexpr int kOrientChunks = 8;
 
+// The oriented graph is built in the caller's numbering: on an engine that
+// renumbered its vertices (inv non-null: engine vertex u is the caller's
+// inv[u]) the ids are mapped back while the lists are read, so N+ keeps the
+// input's ascending id order and the counting kernels below index by the
+// caller's ids.  deg stays in the engine's numbering.
+
 // |N+(u)| per vertex.
 __global__ void tc_count_kernel(const int64_t* __restrict__ off, const int32_t* __restrict__ col,
-                                const int32_t* __restrict__ deg, int32_t V, int32_t* __restrict__ cnt) {
+                                const int32_t* __restrict__ deg, const int32_t* __restrict__ inv, int32_t V,
+                                int32_t* __restrict__ cnt) {
   const int lane = threadIdx.x & 31;
   const int warps = gridDim.x * (blockDim.x >> 5);
   for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < V; u += warps) {
     const int32_t du = deg[u];
+    const int32_t uo = inv ? inv[u] : u;
     const int64_t e1 = off[u + 1];
     int c = 0;
     for (int64_t base = off[u]; base < e1; base += 32 * kOrientChunks) {
@@ -70,26 +78,31 @@ __global__ void tc_count_kernel(const int64_t* __restrict__ off, const int32_t* 
       for (int j = 0; j < kOrientChunks; ++j) v[j] = base + 32 * j + lane < e1 ? col[base + 32 * j + lane] : 0;
 #pragma unroll
       for (int j = 0; j < kOrientChunks; ++j) dv[j] = base + 32 * j + lane < e1 ? deg[v[j]] : 0;
+      if (inv) {
 #pragma unroll
-      for (int j = 0; j < kOrientChunks; ++j) c += base + 32 * j + lane < e1 && tc_before(du, u, dv[j], v[j]);
+        for (int j = 0; j < kOrientChunks; ++j) v[j] = inv[v[j]];
+      }
+#pragma unroll
+      for (int j = 0; j < kOrientChunks; ++j) c += base + 32 * j + lane < e1 && tc_before(du, uo, dv[j], v[j]);
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-    if (lane == 0) cnt[u] = c;
+    if (lane == 0) cnt[uo] = c;
   }
 }
 
 // N+(u), in the input's ascending order: chunk by chunk, ballot + popc
 // compaction.
 __global__ void tc_fill_kernel(const int64_t* __restrict__ off, const int32_t* __restrict__ col,
-                               const int32_t* __restrict__ deg, int32_t V, const int64_t* __restrict__ doff,
-                               int32_t* __restrict__ dcol) {
+                               const int32_t* __restrict__ deg, const int32_t* __restrict__ inv, int32_t V,
+                               const int64_t* __restrict__ doff, int32_t* __restrict__ dcol) {
   const int lane = threadIdx.x & 31;
   const unsigned below = (1u << lane) - 1u;
   const int warps = gridDim.x * (blockDim.x >> 5);
   for (int u = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < V; u += warps) {
     const int32_t du = deg[u];
-    int64_t pos = doff[u];
+    const int32_t uo = inv ? inv[u] : u;
+    int64_t pos = doff[uo];
     const int64_t e1 = off[u + 1];
     for (int64_t base = off[u]; base < e1; base += 32 * kOrientChunks) {
       int32_t v[kOrientChunks], dv[kOrientChunks];
@@ -97,9 +110,13 @@ __global__ void tc_fill_kernel(const int64_t* __restrict__ off, const int32_t* _
       for (int j = 0; j < kOrientChunks; ++j) v[j] = base + 32 * j + lane < e1 ? col[base + 32 * j + lane] : 0;
 #pragma unroll
       for (int j = 0; j < kOrientChunks; ++j) dv[j] = base + 32 * j + lane < e1 ? deg[v[j]] : 0;
+      if (inv) {
+#pragma unroll
+        for (int j = 0; j < kOrientChunks; ++j) v[j] = inv[v[j]];
+      }
 #pragma unroll
       for (int j = 0; j < kOrientChunks; ++j) {
-        const bool keep = base + 32 * j + lane < e1 && tc_before(du, u, dv[j], v[j]);
+        const bool keep = base + 32 * j + lane < e1 && tc_before(du, uo, dv[j], v[j]);
         const unsigned m = __ballot_sync(0xffffffffu, keep);
         if (keep) dcol[pos + __popc(m & below)] = v[j];
         pos += __popc(m);
@@ -350,7 +367,8 @@ extern "C" gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_sta
   GX_TRY(dev_alloc(&b.ctr, 2));  // claim counters of the warp and CTA kernels
   const int grid = e->n_sm * 8;
   tc_degree_kernel<<<grid, 256, 0, s>>>(e->d_off, V, b.deg);
-  tc_count_kernel<<<grid, 256, 0, s>>>(e->d_off, e->d_col, b.deg, V, b.cnt);
+  const int32_t* inv = e->relabeled ? e->d_inv : nullptr;
+  tc_count_kernel<<<grid, 256, 0, s>>>(e->d_off, e->d_col, b.deg, inv, V, b.cnt);
   GX_CUDA(cudaGetLastError());
   // Offsets of N+ and the claim order (descending |N+|, by power-of-two bins).
   // Host buffers are not zero-filled (every element is written below) and are
@@ -416,7 +434,7 @@ extern "C" gx_status gx_triangle_count(gx_engine* e, uint64_t* total, gx_run_sta
   GX_CUDA(cudaMemcpyAsync(b.doff, doff.get(), sizeof(int64_t) * (V + 1), cudaMemcpyHostToDevice, s));
   if (n_order > 0)
     GX_CUDA(cudaMemcpyAsync(b.order, order.get(), sizeof(int32_t) * n_order, cudaMemcpyHostToDevice, s));
-  tc_fill_kernel<<<grid, 256, 0, s>>>(e->d_off, e->d_col, b.deg, V, b.doff, b.dcol);
+  tc_fill_kernel<<<grid, 256, 0, s>>>(e->d_off, e->d_col, b.deg, inv, V, b.doff, b.dcol);
   GX_CUDA(cudaMemsetAsync(b.out, 0, 2 * sizeof(unsigned long long), s));
   GX_CUDA(cudaMemsetAsync(b.ctr, 0, 2 * sizeof(unsigned int), s));
   // The long lists run on the copy stream beside the warp kernel, so the
