@@ -190,34 +190,44 @@ void relabel_host(gx_engine* e) {
   int32_t* inv = e->h_inv.data();
   int32_t* perm = e->h_perm.data();
   constexpr int kKeys = 4096;
-#pragma omp parallel for schedule(dynamic, 1)
-  for (int32_t p = 0; p < P; ++p) {
-    const int32_t b = e->bounds[p], t = e->bounds[p + 1];
-    std::vector<int32_t> start(kKeys + 1, 0);
-    auto key = [&](int32_t v) {  // descending in-degree: key 0 is the largest
-      // (clamped at 0: the device has not yet checked that off is monotone)
-      const int64_t d = std::max<int64_t>(off[v + 1] - off[v], 0);
-      return kKeys - 1 - static_cast<int>(d < kKeys - 1 ? d : kKeys - 1);
-    };
-    for (int32_t v = b; v < t; ++v) ++start[key(v) + 1];
-    for (int k = 0; k < kKeys; ++k) start[k + 1] += start[k];
-    for (int32_t v = b; v < t; ++v) inv[b + start[key(v)]++] = v;
+  // (clamped at 0: the device has not yet checked that off is monotone)
+  auto key = [&](int32_t v) {  // descending in-degree: key 0 is the largest
+    const int64_t d = std::max<int64_t>(off[v + 1] - off[v], 0);
+    return kKeys - 1 - static_cast<int>(d < kKeys - 1 ? d : kKeys - 1);
+  };
+#pragma omp parallel
+  {
+    std::vector<int32_t> start(kKeys + 1);
+#pragma omp for schedule(dynamic, 1)
+    for (int32_t p = 0; p < P; ++p) {
+      const int32_t b = e->bounds[p], t = e->bounds[p + 1];
+      std::fill(start.begin(), start.end(), 0);
+      for (int32_t v = b; v < t; ++v) ++start[key(v) + 1];
+      for (int k = 0; k < kKeys; ++k) start[k + 1] += start[k];
+      for (int32_t v = b; v < t; ++v) inv[b + start[key(v)]++] = v;
+    }
   }
   hvec<int64_t> noff(static_cast<size_t>(V) + 1);
   hvec<int32_t> nod(static_cast<size_t>(V));
   std::vector<int64_t> part;
+  std::vector<std::vector<int32_t>> longs;
 #pragma omp parallel
   {
     const int nt = omp_get_num_threads(), t = omp_get_thread_num();
 #pragma omp single
-    part.assign(static_cast<size_t>(nt) + 1, 0);
+    {
+      part.assign(static_cast<size_t>(nt) + 1, 0);
+      longs.assign(static_cast<size_t>(nt), {});
+    }
     const int64_t lo = static_cast<int64_t>(V) * t / nt, hi = static_cast<int64_t>(V) * (t + 1) / nt;
     int64_t sum = 0;
     for (int64_t i = lo; i < hi; ++i) {
       const int32_t v = inv[i];
       perm[v] = static_cast<int32_t>(i);
       nod[i] = e->outdeg[v];
-      sum += off[v + 1] - off[v];
+      const int64_t len = off[v + 1] - off[v];
+      sum += len;
+      if (len > kRelabelWarpMax) longs[t].push_back(static_cast<int32_t>(i));
     }
     part[t + 1] = sum;
 #pragma omp barrier
@@ -231,8 +241,7 @@ void relabel_host(gx_engine* e) {
   }
   noff[V] = off[V];
   e->relabel_longs.clear();
-  for (int32_t i = 0; i < V; ++i)
-    if (noff[i + 1] - noff[i] > kRelabelWarpMax) e->relabel_longs.push_back(i);
+  for (const auto& l : longs) e->relabel_longs.insert(e->relabel_longs.end(), l.begin(), l.end());
   e->off.swap(noff);
   e->outdeg.swap(nod);
 }
@@ -1357,7 +1366,12 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
     GX_TRY(dev_alloc(&e->d_off, static_cast<size_t>(V) + 1));
     GX_CUDA(cudaMemcpy(e->d_off, off, sizeof(int64_t) * (V + 1), cudaMemcpyHostToDevice));
   }
-  if (!(direct && outdeg) || relabel) {
+  if (relabel) {
+    // On the copy stream behind the other uploads (the host copy lives in
+    // the engine).
+    GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
+    GX_TRY(upload_async(e, e->d_outdeg, e->outdeg.data(), sizeof(int32_t) * static_cast<size_t>(V), e->s_copy));
+  } else if (!(direct && outdeg)) {
     GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
     GX_CUDA(cudaMemcpy(e->d_outdeg, e->outdeg.data(), sizeof(int32_t) * V, cudaMemcpyHostToDevice));
   }

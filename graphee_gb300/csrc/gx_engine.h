@@ -225,7 +225,8 @@ struct gx_engine {
   // gx_set_weights; d_stage carries values between the two numberings;
   // relabel_longs lists the new vertices whose in-lists a CTA rewrites.
   bool relabeled = false;
-  std::vector<int32_t> h_perm, h_inv, relabel_longs;
+  gx::hvec<int32_t> h_perm, h_inv;
+  std::vector<int32_t> relabel_longs;
   int32_t* d_perm = nullptr;
   int32_t* d_inv = nullptr;
   int32_t* d_longs = nullptr;
