@@ -414,6 +414,47 @@ gx_status begin_build(int32_t device, BuildBuffers& B, int* n_sm) {
 
 }  // namespace
 
+namespace gx {
+
+void radix_scratch_sizes(int64_t n, int64_t* hist_elems, int64_t* part_elems) {
+  const int64_t n_tiles = std::max<int64_t>((n + kRadixTile - 1) / kRadixTile, 1);
+  *hist_elems = 256 * n_tiles;
+  *part_elems = std::max<int64_t>((256 * n_tiles + kScanTile - 1) / kScanTile, (n + kScanTile - 1) / kScanTile) + 1;
+}
+
+gx_status radix_sort_bits(unsigned long long* keys, unsigned long long* tmp, int64_t n, int lo_bit, int hi_bit,
+                          uint32_t* hist, unsigned long long* offs, unsigned long long* part, cudaStream_t s,
+                          unsigned long long** sorted) {
+  unsigned long long* buf[2] = {keys, tmp};
+  int cur = 0;
+  if (n > 0) {
+    const int64_t n_tiles = (n + kRadixTile - 1) / kRadixTile;
+    if (n_tiles > INT32_MAX / 2) return fail(GX_ERR_INVALID, "radix sort: %lld keys are too many", (long long)n);
+    for (int shift = lo_bit; shift < hi_bit; shift += 8) {
+      radix_hist_kernel<<<static_cast<unsigned>(n_tiles), kBuildThreads, 0, s>>>(buf[cur], n, shift, hist, n_tiles);
+      GX_TRY(scan_u32(hist, 256 * n_tiles, offs, part, s));
+      radix_scatter_kernel<<<static_cast<unsigned>(n_tiles), kBuildThreads, 0, s>>>(buf[cur], buf[cur ^ 1], n, shift,
+                                                                                  offs, n_tiles);
+      GX_CUDA(cudaGetLastError());
+      cur ^= 1;
+    }
+  }
+  *sorted = buf[cur];
+  return GX_OK;
+}
+
+gx_status scan_u32(const uint32_t* in, int64_t m, unsigned long long* out, unsigned long long* part, cudaStream_t s) {
+  if (m <= 0) return GX_OK;
+  const int64_t nb = (m + kScanTile - 1) / kScanTile;
+  scan_partial_kernel<<<static_cast<unsigned>(nb), kBuildThreads, 0, s>>>(in, m, part);
+  scan_partials_kernel<<<1, kBuildThreads, 0, s>>>(part, nb);
+  scan_final_kernel<<<static_cast<unsigned>(nb), kBuildThreads, 0, s>>>(in, m, part, out);
+  GX_CUDA(cudaGetLastError());
+  return GX_OK;
+}
+
+}  // namespace gx
+
 extern "C" {
 
 gx_status gx_build_csc_gpu(int32_t device, int32_t V, int64_t n, const int32_t* src, const int32_t* dst,

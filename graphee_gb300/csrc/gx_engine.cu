@@ -174,93 +174,9 @@ void build_units(gx_engine* e) {
   e->n_partials = n_part[P];
 }
 
-// Longest in-list a warp rewrites when the engine relabels; longer ones go
-// to a CTA each.
+// Longest in-list a warp moves when the engine relabels; longer ones go to
+// the CTAs of relabel_scatter_long_kernel.
 constexpr int64_t kRelabelWarpMax = 65536;
-
-// The relabelling order on the host: in each shard, the vertices by
-// descending in-degree (capped at 4095, stable in the caller's numbering), by
-// a counting sort per shard.  Fills h_inv / h_perm and turns e->off and
-// e->outdeg into the new numbering.
-void relabel_host(gx_engine* e) {
-  const int32_t V = e->V, P = e->P;
-  const int64_t* off = e->off.data();
-  e->h_inv.resize(static_cast<size_t>(V));
-  e->h_perm.resize(static_cast<size_t>(V));
-  int32_t* inv = e->h_inv.data();
-  int32_t* perm = e->h_perm.data();
-  constexpr int kKeys = 4096;
-  // (clamped at 0: the device has not yet checked that off is monotone)
-  auto key = [&](int32_t v) {  // descending in-degree: key 0 is the largest
-    const int64_t d = std::max<int64_t>(off[v + 1] - off[v], 0);
-    return kKeys - 1 - static_cast<int>(d < kKeys - 1 ? d : kKeys - 1);
-  };
-#pragma omp parallel
-  {
-    std::vector<int32_t> start(kKeys + 1);
-#pragma omp for schedule(dynamic, 1)
-    for (int32_t p = 0; p < P; ++p) {
-      const int32_t b = e->bounds[p], t = e->bounds[p + 1];
-      std::fill(start.begin(), start.end(), 0);
-      for (int32_t v = b; v < t; ++v) ++start[key(v) + 1];
-      for (int k = 0; k < kKeys; ++k) start[k + 1] += start[k];
-      for (int32_t v = b; v < t; ++v) inv[b + start[key(v)]++] = v;
-    }
-  }
-  hvec<int64_t> noff(static_cast<size_t>(V) + 1);
-  hvec<int32_t> nod(static_cast<size_t>(V));
-  std::vector<int64_t> part;
-  std::vector<std::vector<int32_t>> longs;
-#pragma omp parallel
-  {
-    const int nt = omp_get_num_threads(), t = omp_get_thread_num();
-#pragma omp single
-    {
-      part.assign(static_cast<size_t>(nt) + 1, 0);
-      longs.assign(static_cast<size_t>(nt), {});
-    }
-    const int64_t lo = static_cast<int64_t>(V) * t / nt, hi = static_cast<int64_t>(V) * (t + 1) / nt;
-    int64_t sum = 0;
-    for (int64_t i = lo; i < hi; ++i) {
-      const int32_t v = inv[i];
-      perm[v] = static_cast<int32_t>(i);
-      nod[i] = e->outdeg[v];
-      const int64_t len = off[v + 1] - off[v];
-      sum += len;
-      if (len > kRelabelWarpMax) longs[t].push_back(static_cast<int32_t>(i));
-    }
-    part[t + 1] = sum;
-#pragma omp barrier
-#pragma omp single
-    for (int i = 0; i < nt; ++i) part[i + 1] += part[i];
-    int64_t run = part[t];
-    for (int64_t i = lo; i < hi; ++i) {
-      noff[i] = run;
-      run += off[inv[i] + 1] - off[inv[i]];
-    }
-  }
-  noff[V] = off[V];
-  e->relabel_longs.clear();
-  for (const auto& l : longs) e->relabel_longs.insert(e->relabel_longs.end(), l.begin(), l.end());
-  e->off.swap(noff);
-  e->outdeg.swap(nod);
-}
-
-// Rewrites per-edge data laid out by the caller's offsets (d_off_old) into
-// the relabelled layout: source ids renamed through d_perm (perm = true), or
-// values copied (weights).
-gx_status relabel_device_lists(gx_engine* e, const int32_t* src, int32_t* dst, bool perm, cudaStream_t s) {
-  relabel_lists_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, src, e->d_off, e->d_inv, perm ? e->d_perm : nullptr,
-                                                   e->V, kRelabelWarpMax, dst);
-  GX_CUDA(cudaGetLastError());
-  if (!e->relabel_longs.empty()) {
-    relabel_long_kernel<<<static_cast<int>(e->relabel_longs.size()), 1024, 0, s>>>(
-        e->d_off_old, src, e->d_off, e->d_inv, perm ? e->d_perm : nullptr, e->d_longs, dst);
-    GX_CUDA(cudaGetLastError());
-  }
-  GX_CUDA(cudaStreamSynchronize(s));
-  return GX_OK;
-}
 
 // Values in the caller's numbering from the engine's buffer (d_stage).
 gx_status values_to_caller(gx_engine* e, const void* d_vals, cudaStream_t s) {
@@ -307,6 +223,173 @@ gx_status upload_async(gx_engine* e, void* dst, const void* src, size_t bytes, c
   } else {
     GX_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
   }
+  return GX_OK;
+}
+
+// Device-to-host copy into a host array on `s`: written in place by a kernel
+// when the device can reach pageable memory.
+gx_status download_async(gx_engine* e, void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return GX_OK;
+  if (e->pageable_access && (reinterpret_cast<uintptr_t>(dst) & 3u) == 0 && bytes % 4 == 0) {
+    host_copy_kernel<<<e->n_sm * 8, 256, 0, s>>>(src, dst, bytes);
+    GX_CUDA(cudaGetLastError());
+  } else {
+    GX_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, s));
+  }
+  return GX_OK;
+}
+
+// Host pages of a large array that the device is about to write in place are
+// placed by the host threads first (a device write to an unmapped host page
+// would fault it in from the device side, one page at a time).
+template <class T>
+void host_resize_placed(hvec<T>& v, size_t n) {
+  const bool fresh = v.capacity() < n;
+  v.resize(n);
+  if (!fresh) return;
+  T* p = v.data();
+#pragma omp parallel for schedule(static)
+  for (int64_t i = 0; i < static_cast<int64_t>(n); ++i) p[i] = T();
+}
+
+// Lists longer than kRelabelWarpMax in a valid CSC of E edges.
+unsigned int relabel_longs_cap(int64_t E) { return static_cast<unsigned int>(E / kRelabelWarpMax + 1); }
+
+// Enqueues the move of per-edge data (source ids, renamed, or weights) from
+// the caller's layout to the relabelled one (relabel_scatter_kernel).
+gx_status relabel_scatter(gx_engine* e, const int32_t* src, int32_t* dst, bool rename, int32_t* longs,
+                          unsigned int* n_longs, unsigned int* flag, cudaStream_t s) {
+  const unsigned int cap = relabel_longs_cap(e->E);
+  GX_CUDA(cudaMemsetAsync(n_longs, 0, sizeof(unsigned int), s));
+  relabel_scatter_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, src, e->d_off, e->d_perm,
+                                                     rename ? e->d_perm : nullptr, e->V, e->E, kRelabelWarpMax, dst,
+                                                     longs, cap, n_longs, flag);
+  relabel_scatter_long_kernel<<<e->n_sm * 2, 1024, 0, s>>>(e->d_off_old, src, e->d_off, e->d_perm,
+                                                           rename ? e->d_perm : nullptr, e->V, dst, longs, cap,
+                                                           n_longs, flag);
+  GX_CUDA(cudaGetLastError());
+  return GX_OK;
+}
+
+// Buffers of one load, freed once the copy stream is idle.
+struct LoadScratch {
+  cudaStream_t s;
+  unsigned int* flag = nullptr;
+  int32_t* col_old = nullptr;
+  int32_t* od_old = nullptr;
+  uint32_t* len = nullptr;
+  unsigned long long* keys[2] = {nullptr, nullptr};
+  uint32_t* hist = nullptr;
+  unsigned long long* offs = nullptr;
+  unsigned long long* part = nullptr;
+  int32_t* longs = nullptr;
+  unsigned int* n_longs = nullptr;
+  hvec<int32_t> od_host;  // out-degrees computed on the host, read by the device in place
+  explicit LoadScratch(cudaStream_t st) : s(st) {}
+  ~LoadScratch() {
+    if (flag || col_old || keys[0]) cudaStreamSynchronize(s);
+    dev_free(&flag);
+    dev_free(&col_old);
+    dev_free(&od_old);
+    dev_free(&len);
+    dev_free(&keys[0]);
+    dev_free(&keys[1]);
+    dev_free(&hist);
+    dev_free(&offs);
+    dev_free(&part);
+    dev_free(&longs);
+    dev_free(&n_longs);
+  }
+};
+
+int bits_for(int64_t n) {  // bits of the largest value below n
+  int b = 1;
+  while (b < 62 && (int64_t(1) << b) < n) ++b;
+  return b;
+}
+
+__global__ void store_i64_kernel(int64_t* p, int64_t x) { *p = x; }
+
+// A relabelling load up to the move of the source ids: the caller's offsets
+// go to the device, which sorts the vertices into the new order, derives the
+// new offsets and out-degrees, copies them and the permutation back for the
+// host's own planning (e->off, e->outdeg, h_perm: waited for here), and then
+// streams the caller's source ids once, renaming them into place (still
+// running on the copy stream when this returns; flag bits as
+// validate_csc_kernel's).  Also counts the dangling vertices.
+gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, const int32_t* col,
+                       const int32_t* outdeg, LoadScratch& sc) {
+  const int32_t V = e->V, P = e->P;
+  const int64_t E = e->E;
+  cudaStream_t s = e->s_copy;
+  const int vb = bits_for(V), pb = bits_for(P);
+  GX_TRY(dev_alloc(&e->d_off, static_cast<size_t>(V) + 1));
+  GX_TRY(dev_alloc(&e->d_col, static_cast<size_t>(E) + 8));
+  GX_TRY(dev_alloc(&e->d_off_old, static_cast<size_t>(V) + 1));
+  GX_TRY(dev_alloc(&e->d_bounds, static_cast<size_t>(P) + 1));
+  GX_TRY(dev_alloc(&e->d_perm, static_cast<size_t>(V)));
+  GX_TRY(dev_alloc(&e->d_inv, static_cast<size_t>(V)));
+  GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
+  GX_TRY(dev_alloc(&e->d_stage, static_cast<size_t>(V)));
+  GX_TRY(dev_alloc(&sc.keys[0], static_cast<size_t>(V)));
+  GX_TRY(dev_alloc(&sc.keys[1], static_cast<size_t>(V)));
+  GX_TRY(dev_alloc(&sc.len, static_cast<size_t>(V)));
+  GX_TRY(dev_alloc(&sc.od_old, static_cast<size_t>(V)));
+  int64_t hist_n = 0, part_n = 0;
+  radix_scratch_sizes(V, &hist_n, &part_n);
+  GX_TRY(dev_alloc(&sc.hist, static_cast<size_t>(hist_n)));
+  GX_TRY(dev_alloc(&sc.offs, static_cast<size_t>(hist_n)));
+  GX_TRY(dev_alloc(&sc.part, static_cast<size_t>(part_n)));
+  GX_TRY(dev_alloc(&sc.longs, relabel_longs_cap(E)));
+  GX_TRY(dev_alloc(&sc.n_longs, 1));
+  GX_TRY(dev_alloc(&sc.flag, 1));
+  GX_CUDA(cudaMemsetAsync(sc.flag, 0, sizeof(unsigned int), s));
+  GX_CUDA(cudaMemsetAsync(e->d_col + E, 0, 8 * sizeof(int32_t), s));
+  GX_TRY(upload_async(e, e->d_off_old, off, sizeof(int64_t) * (static_cast<size_t>(V) + 1), s));
+  GX_CUDA(cudaMemcpyAsync(e->d_bounds, bounds, sizeof(int32_t) * (P + 1), cudaMemcpyHostToDevice, s));
+  validate_csc_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, V, nullptr, E, sc.flag);
+  relabel_keys_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, e->d_bounds, P, V, vb, sc.keys[0]);
+  GX_CUDA(cudaGetLastError());
+  unsigned long long* sorted = nullptr;
+  GX_TRY(radix_sort_bits(sc.keys[0], sc.keys[1], V, vb, vb + 12 + pb, sc.hist, sc.offs, sc.part, s, &sorted));
+  // Out-degrees in the caller's numbering (while the device sorts).
+  const int32_t* od = outdeg;
+  if (!od) {
+    sc.od_host.resize(static_cast<size_t>(V));
+    GX_TRY(gx_out_degree(V, off, col, sc.od_host.data()));
+    od = sc.od_host.data();
+  }
+  int64_t n_dang = 0;
+#pragma omp parallel for reduction(+ : n_dang)
+  for (int32_t v = 0; v < V; ++v) n_dang += od[v] == 0;
+  e->n_dangling = n_dang;
+  GX_TRY(upload_async(e, sc.od_old, od, sizeof(int32_t) * static_cast<size_t>(V), s));
+  relabel_order_kernel<<<e->n_sm * 8, 256, 0, s>>>(sorted, (1ull << vb) - 1, V, e->d_off_old, sc.od_old, e->d_inv,
+                                                   e->d_perm, e->d_outdeg, sc.len);
+  GX_CUDA(cudaGetLastError());
+  GX_TRY(scan_u32(sc.len, V, reinterpret_cast<unsigned long long*>(e->d_off), sc.part, s));
+  store_i64_kernel<<<1, 1, 0, s>>>(e->d_off + V, E);
+  // The host's copies in the new numbering.
+  host_resize_placed(e->off, static_cast<size_t>(V) + 1);
+  host_resize_placed(e->outdeg, static_cast<size_t>(V));
+  host_resize_placed(e->h_perm, static_cast<size_t>(V));
+  GX_TRY(download_async(e, e->off.data(), e->d_off, sizeof(int64_t) * (static_cast<size_t>(V) + 1), s));
+  GX_TRY(download_async(e, e->outdeg.data(), e->d_outdeg, sizeof(int32_t) * static_cast<size_t>(V), s));
+  GX_TRY(download_async(e, e->h_perm.data(), e->d_perm, sizeof(int32_t) * static_cast<size_t>(V), s));
+  cudaEvent_t ev = nullptr;
+  GX_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  std::unique_ptr<CUevent_st, cudaError_t (*)(cudaEvent_t)> evg(ev, cudaEventDestroy);
+  GX_CUDA(cudaEventRecord(ev, s));
+  // The source ids: read in place from the caller's array where the device
+  // can, else uploaded first.
+  const int32_t* src = col;
+  if (!e->pageable_access && E > 0) {
+    GX_TRY(dev_alloc(&sc.col_old, static_cast<size_t>(E)));
+    GX_CUDA(cudaMemcpyAsync(sc.col_old, col, sizeof(int32_t) * E, cudaMemcpyHostToDevice, s));
+    src = sc.col_old;
+  }
+  GX_TRY(relabel_scatter(e, src, e->d_col, true, sc.longs, sc.n_longs, sc.flag, s));
+  GX_CUDA(cudaEventSynchronize(ev));
   return GX_OK;
 }
 
@@ -1264,76 +1347,49 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   // out-degrees and the source ids go to the device at once, on the copy
   // stream, while the host prepares the work units below.
   const bool direct = e->cfg.cache_budget_bytes < 0;
-  // Small device buffers of the load; freed once the copy stream is idle.
-  // Relabelling (config.relabel): the caller's offsets and ids go to the
-  // device as they are, are checked there, and are rewritten into the new
-  // numbering once the host has computed it.
-  const bool relabel = direct && e->cfg.relabel != 0;
-  struct Scratch {
-    cudaStream_t s;
-    unsigned int* flag = nullptr;
-    int32_t* col_old = nullptr;
-    ~Scratch() {
-      if (flag || col_old) cudaStreamSynchronize(s);
-      dev_free(&flag);
-      dev_free(&col_old);
-    }
-  } scratch{e->s_copy};
-  if (direct) {
+  // Relabelling (config.relabel) for resident loads whose sort keys (shard,
+  // degree rank, vertex id) fit 64 bits and whose lists fit 32-bit lengths.
+  const bool relabel = direct && e->cfg.relabel != 0 && bits_for(V) + 12 + bits_for(P) <= 64 &&
+                       E <= static_cast<int64_t>(UINT32_MAX);
+  LoadScratch scratch(e->s_copy);
+  if (relabel) {
+    GX_TRY(relabel_load(e, bounds, off, col, outdeg, scratch));
+    phase("relabelled");
+  } else if (direct) {
     GX_TRY(dev_alloc(&e->d_off, static_cast<size_t>(V) + 1));
     GX_TRY(dev_alloc(&e->d_col, static_cast<size_t>(E) + 8));
     GX_CUDA(cudaMemsetAsync(e->d_col + E, 0, 8 * sizeof(int32_t), e->s_copy));
-    int64_t* up_off = e->d_off;
-    int32_t* up_col = e->d_col;
-    if (relabel) {
-      GX_TRY(dev_alloc(&e->d_off_old, static_cast<size_t>(V) + 1));
-      GX_TRY(dev_alloc(&scratch.col_old, static_cast<size_t>(E) + 8));
-      up_off = e->d_off_old;
-      up_col = scratch.col_old;
-    }
-    GX_TRY(upload_async(e, up_off, off, sizeof(int64_t) * (static_cast<size_t>(V) + 1), e->s_copy));
-    GX_TRY(upload_async(e, up_col, col, sizeof(int32_t) * static_cast<size_t>(E), e->s_copy));
-    if (outdeg && !relabel) {
+    GX_TRY(upload_async(e, e->d_off, off, sizeof(int64_t) * (static_cast<size_t>(V) + 1), e->s_copy));
+    GX_TRY(upload_async(e, e->d_col, col, sizeof(int32_t) * static_cast<size_t>(E), e->s_copy));
+    if (outdeg) {
       GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
       GX_TRY(upload_async(e, e->d_outdeg, outdeg, sizeof(int32_t) * static_cast<size_t>(V), e->s_copy));
     }
     // Behind the uploads: the load-time checks.
     GX_TRY(dev_alloc(&scratch.flag, 1));
     GX_CUDA(cudaMemsetAsync(scratch.flag, 0, sizeof(unsigned int), e->s_copy));
-    validate_csc_kernel<<<e->n_sm * 8, 256, 0, e->s_copy>>>(up_off, V, up_col, E, scratch.flag);
+    validate_csc_kernel<<<e->n_sm * 8, 256, 0, e->s_copy>>>(e->d_off, V, e->d_col, E, scratch.flag);
     GX_CUDA(cudaGetLastError());
   }
   e->bounds.assign(bounds, bounds + P + 1);
-  e->off.resize(static_cast<size_t>(V) + 1);
-  e->outdeg.resize(static_cast<size_t>(V));
-  int64_t* hoff = e->off.data();
+  if (!relabel) {
+    e->off.resize(static_cast<size_t>(V) + 1);
+    e->outdeg.resize(static_cast<size_t>(V));
+    int64_t* hoff = e->off.data();
 #pragma omp parallel for schedule(static)
-  for (int64_t v = 0; v <= V; ++v) hoff[v] = off[v];
-  if (outdeg) {
-    int32_t* hod = e->outdeg.data();
+    for (int64_t v = 0; v <= V; ++v) hoff[v] = off[v];
+    if (outdeg) {
+      int32_t* hod = e->outdeg.data();
 #pragma omp parallel for schedule(static)
-    for (int64_t v = 0; v < V; ++v) hod[v] = outdeg[v];
-  } else {
-    gx_status st = gx_out_degree(V, off, col, e->outdeg.data());
-    if (st != GX_OK) return st;
-  }
-  int64_t n_dang = 0;
+      for (int64_t v = 0; v < V; ++v) hod[v] = outdeg[v];
+    } else {
+      gx_status st = gx_out_degree(V, off, col, e->outdeg.data());
+      if (st != GX_OK) return st;
+    }
+    int64_t n_dang = 0;
 #pragma omp parallel for reduction(+ : n_dang)
-  for (int32_t v = 0; v < V; ++v) n_dang += e->outdeg[v] == 0;
-  e->n_dangling = n_dang;
-  if (relabel) {
-    relabel_host(e);
-    phase("relabelled");
-    GX_TRY(upload_async(e, e->d_off, e->off.data(), sizeof(int64_t) * (static_cast<size_t>(V) + 1), e->s_copy));
-    GX_TRY(dev_alloc(&e->d_perm, static_cast<size_t>(V)));
-    GX_TRY(dev_alloc(&e->d_inv, static_cast<size_t>(V)));
-    GX_TRY(dev_alloc(&e->d_longs, std::max<size_t>(e->relabel_longs.size(), 1)));
-    GX_TRY(dev_alloc(&e->d_stage, static_cast<size_t>(V)));
-    GX_TRY(upload_async(e, e->d_perm, e->h_perm.data(), sizeof(int32_t) * static_cast<size_t>(V), e->s_copy));
-    GX_TRY(upload_async(e, e->d_inv, e->h_inv.data(), sizeof(int32_t) * static_cast<size_t>(V), e->s_copy));
-    if (!e->relabel_longs.empty())
-      GX_CUDA(cudaMemcpyAsync(e->d_longs, e->relabel_longs.data(), sizeof(int32_t) * e->relabel_longs.size(),
-                              cudaMemcpyHostToDevice, e->s_copy));
+    for (int32_t v = 0; v < V; ++v) n_dang += e->outdeg[v] == 0;
+    e->n_dangling = n_dang;
   }
   // With a shard-cache budget not every shard reaches the device: check the
   // source ids on the host.  Otherwise the device checks them after the
@@ -1366,12 +1422,7 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
     GX_TRY(dev_alloc(&e->d_off, static_cast<size_t>(V) + 1));
     GX_CUDA(cudaMemcpy(e->d_off, off, sizeof(int64_t) * (V + 1), cudaMemcpyHostToDevice));
   }
-  if (relabel) {
-    // On the copy stream behind the other uploads (the host copy lives in
-    // the engine).
-    GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
-    GX_TRY(upload_async(e, e->d_outdeg, e->outdeg.data(), sizeof(int32_t) * static_cast<size_t>(V), e->s_copy));
-  } else if (!(direct && outdeg)) {
+  if (!relabel && !(direct && outdeg)) {
     GX_TRY(dev_alloc(&e->d_outdeg, static_cast<size_t>(V)));
     GX_CUDA(cudaMemcpy(e->d_outdeg, e->outdeg.data(), sizeof(int32_t) * V, cudaMemcpyHostToDevice));
   }
@@ -1416,12 +1467,7 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
       e->release_graph();
       return fail(GX_ERR_INVALID, "gx_load_csc: source id outside [0, %d)", V);
     }
-    if (relabel) {
-      // The ids are in range: rename them into the new numbering.
-      GX_TRY(relabel_device_lists(e, scratch.col_old, e->d_col, true, e->s_copy));
-      e->relabeled = true;
-      phase("rewritten");
-    }
+    e->relabeled = relabel;
   }
   GX_TRY(plan_shards(e, src_col, direct));
   if (!direct) {
@@ -1449,8 +1495,10 @@ gx_status gx_load_csc(gx_engine* e, int32_t V, int32_t P, const int32_t* bounds,
   // Shard bounds and bitmaps of the selective steps; the changed-vertex list
   // that streamed graphs hand to the host (a selective step changes fewer
   // than BF_THRE * V vertices).
-  GX_TRY(dev_alloc(&e->d_bounds, static_cast<size_t>(P) + 1));
-  GX_CUDA(cudaMemcpy(e->d_bounds, bounds, sizeof(int32_t) * (P + 1), cudaMemcpyHostToDevice));
+  if (!relabel) {
+    GX_TRY(dev_alloc(&e->d_bounds, static_cast<size_t>(P) + 1));
+    GX_CUDA(cudaMemcpy(e->d_bounds, bounds, sizeof(int32_t) * (P + 1), cudaMemcpyHostToDevice));
+  }
   GX_TRY(dev_alloc(&e->d_shard_bm, 2 * static_cast<size_t>((P + 31) / 32)));
   if (!e->all_resident) {
     e->changed_cap = std::max<int64_t>(4096, V / 256);
@@ -1491,14 +1539,19 @@ gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
     GX_TRY(dev_alloc(&e->d_w, static_cast<size_t>(e->E) + 8));
     GX_CUDA(cudaMemsetAsync(e->d_w + e->E, 0, 8 * sizeof(uint32_t), e->s_copy));
     if (e->relabeled) {
-      uint32_t* w_old = nullptr;
-      GX_TRY(dev_alloc(&w_old, static_cast<size_t>(e->E) + 1));
-      gx_status st = upload_async(e, w_old, w, sizeof(uint32_t) * static_cast<size_t>(e->E), e->s_copy);
-      if (st == GX_OK)
-        st = relabel_device_lists(e, reinterpret_cast<const int32_t*>(w_old), reinterpret_cast<int32_t*>(e->d_w),
-                                  false, e->s_copy);
-      gx::pool_free(w_old);
-      GX_TRY(st);
+      LoadScratch sc(e->s_copy);
+      GX_TRY(dev_alloc(&sc.longs, relabel_longs_cap(e->E)));
+      GX_TRY(dev_alloc(&sc.n_longs, 1));
+      GX_TRY(dev_alloc(&sc.flag, 1));
+      GX_CUDA(cudaMemsetAsync(sc.flag, 0, sizeof(unsigned int), e->s_copy));
+      const int32_t* src = reinterpret_cast<const int32_t*>(w);
+      if (!e->pageable_access && e->E > 0) {
+        GX_TRY(dev_alloc(&sc.col_old, static_cast<size_t>(e->E)));
+        GX_CUDA(cudaMemcpyAsync(sc.col_old, w, sizeof(uint32_t) * e->E, cudaMemcpyHostToDevice, e->s_copy));
+        src = sc.col_old;
+      }
+      GX_TRY(relabel_scatter(e, src, reinterpret_cast<int32_t*>(e->d_w), false, sc.longs, sc.n_longs, sc.flag,
+                             e->s_copy));
     } else {
       GX_TRY(upload_async(e, e->d_w, w, sizeof(uint32_t) * static_cast<size_t>(e->E), e->s_copy));
     }

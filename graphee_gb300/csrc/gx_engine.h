@@ -108,6 +108,19 @@ struct UninitAlloc : std::allocator<T> {
 template <class T>
 using hvec = std::vector<T, UninitAlloc<T>>;
 
+// Device sort and scan of the graph build (gx_build.cu), for the engine's
+// load-time relabelling.  radix_scratch_sizes gives the element counts of
+// the scratch for n keys: `hist` and `offs` hold hist_elems each, `part`
+// part_elems.  radix_sort_bits sorts n 64-bit keys stably by bits
+// [lo_bit, hi_bit) (8 a pass; keys and tmp alternate, *sorted is the one
+// holding the result); scan_u32 writes the exclusive prefix sums of m
+// 32-bit counts as 64-bit offsets.  Both only enqueue work on s.
+void radix_scratch_sizes(int64_t n, int64_t* hist_elems, int64_t* part_elems);
+gx_status radix_sort_bits(unsigned long long* keys, unsigned long long* tmp, int64_t n, int lo_bit, int hi_bit,
+                          uint32_t* hist, unsigned long long* offs, unsigned long long* part, cudaStream_t s,
+                          unsigned long long** sorted);
+gx_status scan_u32(const uint32_t* in, int64_t m, unsigned long long* out, unsigned long long* part, cudaStream_t s);
+
 // What a captured superstep graph depends on: the kernels, their launch
 // shapes and their argument bytes (zero-filled before use, padding included).
 struct GraphKey {
@@ -220,16 +233,15 @@ struct gx_engine {
   unsigned int* d_work = nullptr;
   int32_t n_work = 0;
 
-  // Relabelled engine (config.relabel): new vertex i is the caller's vertex
-  // h_inv[i], and h_perm maps back.  d_off_old keeps the caller's offsets for
-  // gx_set_weights; d_stage carries values between the two numberings;
-  // relabel_longs lists the new vertices whose in-lists a CTA rewrites.
+  // Relabelled engine (config.relabel): the caller's vertex v is the
+  // engine's vertex perm[v] (h_perm on the host, d_perm on the device), and
+  // the engine's vertex i is the caller's d_inv[i].  d_off_old keeps the
+  // caller's offsets for gx_set_weights; d_stage carries values between the
+  // two numberings.  e->off and e->outdeg are in the engine's numbering.
   bool relabeled = false;
-  gx::hvec<int32_t> h_perm, h_inv;
-  std::vector<int32_t> relabel_longs;
+  gx::hvec<int32_t> h_perm;
   int32_t* d_perm = nullptr;
   int32_t* d_inv = nullptr;
-  int32_t* d_longs = nullptr;
   int64_t* d_off_old = nullptr;
   uint32_t* d_stage = nullptr;
 
@@ -285,13 +297,10 @@ struct gx_engine {
     gx::dev_free(&d_bm);
     gx::dev_free(&d_perm);
     gx::dev_free(&d_inv);
-    gx::dev_free(&d_longs);
     gx::dev_free(&d_off_old);
     gx::dev_free(&d_stage);
     relabeled = false;
     h_perm.clear();
-    h_inv.clear();
-    relabel_longs.clear();
     gx::dev_free(&d_bounds);
     gx::dev_free(&d_shard_bm);
     gx::dev_free(&d_changed_list);

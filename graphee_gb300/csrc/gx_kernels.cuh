@@ -1110,29 +1110,115 @@ static __global__ void validate_csc_kernel(const int64_t* off, int32_t V, const 
   if (f) atomicOr(flag, f);
 }
 
-// Relabelling: new vertex i is old vertex inv[i].  Its in-list is the old
-// one, in the same order, with every source renamed through perm (perm null:
-// the entries are copied as they are, for weights).  A warp per list, for
-// lists of at most max_len; rel_long_kernel takes the longer ones, a CTA each.
-static __global__ void relabel_lists_kernel(const int64_t* off_old, const int32_t* src, const int64_t* off_new,
-                                            const int32_t* inv, const int32_t* perm, int32_t V, int64_t max_len,
-                                            int32_t* dst) {
-  const int lane = threadIdx.x & 31;
-  const int warps = gridDim.x * (blockDim.x >> 5);
-  for (int32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; i < V; i += warps) {
-    const int32_t v = inv[i];
-    const int64_t b0 = off_old[v], n = off_old[v + 1] - b0, b1 = off_new[i];
-    if (n > max_len) continue;
-    for (int64_t j = lane; j < n; j += 32) dst[b1 + j] = perm ? perm[src[b0 + j]] : src[b0 + j];
+// Relabelling, on the device at load.  The order: within each shard, the
+// vertices by descending in-degree (capped at 4095), ties by ascending id.
+// relabel_keys_kernel writes the sort key of every vertex, its shard and
+// degree rank above `vb` bits of vertex id; a stable sort of those upper
+// bits leaves the keys in the new order.  A length is taken as 0 where off
+// decreases (the load reports that separately).
+static __global__ void relabel_keys_kernel(const int64_t* off, const int32_t* bounds, int32_t P, int32_t V, int vb,
+                                           unsigned long long* keys) {
+  for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+    int32_t lo = 0, hi = P;  // the shard p with bounds[p] <= v < bounds[p + 1]
+    while (hi - lo > 1) {
+      const int32_t mid = (lo + hi) >> 1;
+      if (bounds[mid] <= v) lo = mid;
+      else hi = mid;
+    }
+    const int64_t d = off[v + 1] - off[v];
+    const unsigned long long rank = 4095u - static_cast<unsigned>(d < 0 ? 0 : d > 4095 ? 4095 : d);
+    keys[v] = ((static_cast<unsigned long long>(lo) << 12 | rank) << vb) | static_cast<unsigned long long>(v);
   }
 }
-static __global__ void relabel_long_kernel(const int64_t* off_old, const int32_t* src, const int64_t* off_new,
-                                           const int32_t* inv, const int32_t* perm, const int32_t* longs,
-                                           int32_t* dst) {
-  const int32_t i = longs[blockIdx.x];
-  const int32_t v = inv[i];
-  const int64_t b0 = off_old[v], n = off_old[v + 1] - b0, b1 = off_new[i];
-  for (int64_t j = threadIdx.x; j < n; j += blockDim.x) dst[b1 + j] = perm ? perm[src[b0 + j]] : src[b0 + j];
+
+// From the sorted keys: inv[i] (the old id of new vertex i), perm (its
+// inverse), the out-degree and the in-list length of every new vertex.
+static __global__ void relabel_order_kernel(const unsigned long long* sorted, unsigned long long vmask, int32_t V,
+                                            const int64_t* off_old, const int32_t* outdeg_old, int32_t* inv,
+                                            int32_t* perm, int32_t* outdeg_new, uint32_t* len_new) {
+  for (int32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < V; i += gridDim.x * blockDim.x) {
+    const int32_t v = static_cast<int32_t>(sorted[i] & vmask);
+    inv[i] = v;
+    perm[v] = i;
+    outdeg_new[i] = outdeg_old[v];
+    const int64_t d = off_old[v + 1] - off_old[v];
+    len_new[i] = static_cast<uint32_t>(d < 0 ? 0 : d);
+  }
+}
+
+// Moves per-edge data from the caller's layout to the engine's: old vertex
+// v's list (src[off_old[v], off_old[v+1]), read in order, so the caller's
+// array is streamed once) goes to the new position off_new[perm[v]], with
+// every entry renamed through `rename` (source ids) or copied (rename null:
+// weights).  src may be host memory the device reads in place.  A warp per
+// list of up to max_len entries; longer lists are appended to `longs` for
+// relabel_scatter_long_kernel.  Lists whose offsets leave [0, E] or decrease
+// are skipped (flag bit 0), and out-of-range ids are written as 0 (flag bit
+// 1), so a malformed CSC neither reads nor writes out of bounds.
+static __global__ void relabel_scatter_kernel(const int64_t* off_old, const int32_t* src, const int64_t* off_new,
+                                              const int32_t* perm, const int32_t* rename, int32_t V, int64_t E,
+                                              int64_t max_len, int32_t* dst, int32_t* longs,
+                                              unsigned int longs_cap, unsigned int* n_longs, unsigned int* flag) {
+  const int lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  unsigned int f = 0;
+  for (int32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < V; v += warps) {
+    const int64_t b0 = off_old[v], e0 = off_old[v + 1];
+    if (b0 < 0 || e0 < b0 || e0 > E) {
+      f |= 1u;
+      continue;
+    }
+    const int64_t n = e0 - b0, b1 = off_new[perm[v]];
+    if (b1 < 0 || b1 + n > E) {
+      f |= 1u;
+      continue;
+    }
+    if (n > max_len) {
+      if (lane == 0) {
+        const unsigned int at = atomicAdd(n_longs, 1u);
+        if (at < longs_cap) longs[at] = v;
+        else f |= 1u;  // more long lists than E allows: overlapping lists
+      }
+      continue;
+    }
+    for (int64_t j = lane; j < n; j += 32) {
+      int32_t x = src[b0 + j];
+      if (rename) {
+        if (x < 0 || x >= V) {
+          f |= 2u;
+          x = 0;
+        } else {
+          x = rename[x];
+        }
+      }
+      dst[b1 + j] = x;
+    }
+  }
+  if (f) atomicOr(flag, f);
+}
+static __global__ void relabel_scatter_long_kernel(const int64_t* off_old, const int32_t* src, const int64_t* off_new,
+                                                   const int32_t* perm, const int32_t* rename, int32_t V,
+                                                   int32_t* dst, const int32_t* longs, unsigned int longs_cap,
+                                                   const unsigned int* n_longs, unsigned int* flag) {
+  unsigned int f = 0;
+  const unsigned int n_l = *n_longs < longs_cap ? *n_longs : longs_cap;
+  for (unsigned int l = blockIdx.x; l < n_l; l += gridDim.x) {
+    const int32_t v = longs[l];  // offsets checked by relabel_scatter_kernel
+    const int64_t b0 = off_old[v], n = off_old[v + 1] - b0, b1 = off_new[perm[v]];
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
+      int32_t x = src[b0 + j];
+      if (rename) {
+        if (x < 0 || x >= V) {
+          f |= 2u;
+          x = 0;
+        } else {
+          x = rename[x];
+        }
+      }
+      dst[b1 + j] = x;
+    }
+  }
+  if (f) atomicOr(flag, f);
 }
 // out[v] = in[perm[v]] (values to the caller's numbering), and the inverse.
 static __global__ void gather_values_kernel(const uint32_t* in, const int32_t* perm, int32_t V, uint32_t* out) {
