@@ -312,10 +312,10 @@ __global__ void store_i64_kernel(int64_t* p, int64_t x) { *p = x; }
 
 // A relabelling load up to the move of the source ids: the caller's offsets
 // go to the device, which sorts the vertices into the new order, derives the
-// new offsets and out-degrees, copies them and the permutation back for the
-// host's own planning (e->off, e->outdeg, h_perm: waited for here), and then
-// streams the caller's source ids once, renaming them into place (still
-// running on the copy stream when this returns; flag bits as
+// new offsets and out-degrees, and copies them and the permutation back for
+// the host's own planning (e->off, e->outdeg, h_perm: waited for here); the
+// source ids, uploaded meanwhile, are then renamed into place in one pass
+// (still running on the copy stream when this returns; flag bits as
 // validate_csc_kernel's).  Also counts the dangling vertices.
 gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, const int32_t* col,
                        const int32_t* outdeg, LoadScratch& sc) {
@@ -345,6 +345,15 @@ gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, 
   GX_TRY(dev_alloc(&sc.flag, 1));
   GX_CUDA(cudaMemsetAsync(sc.flag, 0, sizeof(unsigned int), s));
   GX_CUDA(cudaMemsetAsync(e->d_col + E, 0, 8 * sizeof(int32_t), s));
+  // The caller's source ids go up on the compute stream (idle during a load)
+  // while the copy stream works out the order: a device pass that read them
+  // in place list by list would take small, latency-bound host reads.
+  cudaEvent_t ev_col = nullptr;
+  GX_CUDA(cudaEventCreateWithFlags(&ev_col, cudaEventDisableTiming));
+  std::unique_ptr<CUevent_st, cudaError_t (*)(cudaEvent_t)> ev_col_g(ev_col, cudaEventDestroy);
+  GX_TRY(dev_alloc(&sc.col_old, static_cast<size_t>(std::max<int64_t>(E, 1))));
+  GX_TRY(upload_async(e, sc.col_old, col, sizeof(int32_t) * static_cast<size_t>(E), e->s_comp));
+  GX_CUDA(cudaEventRecord(ev_col, e->s_comp));
   GX_TRY(upload_async(e, e->d_off_old, off, sizeof(int64_t) * (static_cast<size_t>(V) + 1), s));
   GX_CUDA(cudaMemcpyAsync(e->d_bounds, bounds, sizeof(int32_t) * (P + 1), cudaMemcpyHostToDevice, s));
   validate_csc_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, V, nullptr, E, sc.flag);
@@ -380,15 +389,8 @@ gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, 
   GX_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   std::unique_ptr<CUevent_st, cudaError_t (*)(cudaEvent_t)> evg(ev, cudaEventDestroy);
   GX_CUDA(cudaEventRecord(ev, s));
-  // The source ids: read in place from the caller's array where the device
-  // can, else uploaded first.
-  const int32_t* src = col;
-  if (!e->pageable_access && E > 0) {
-    GX_TRY(dev_alloc(&sc.col_old, static_cast<size_t>(E)));
-    GX_CUDA(cudaMemcpyAsync(sc.col_old, col, sizeof(int32_t) * E, cudaMemcpyHostToDevice, s));
-    src = sc.col_old;
-  }
-  GX_TRY(relabel_scatter(e, src, e->d_col, true, sc.longs, sc.n_longs, sc.flag, s));
+  GX_CUDA(cudaStreamWaitEvent(s, ev_col, 0));
+  GX_TRY(relabel_scatter(e, sc.col_old, e->d_col, true, sc.longs, sc.n_longs, sc.flag, s));
   GX_CUDA(cudaEventSynchronize(ev));
   return GX_OK;
 }
@@ -1544,13 +1546,9 @@ gx_status gx_set_weights(gx_engine* e, const uint32_t* w) {
       GX_TRY(dev_alloc(&sc.n_longs, 1));
       GX_TRY(dev_alloc(&sc.flag, 1));
       GX_CUDA(cudaMemsetAsync(sc.flag, 0, sizeof(unsigned int), e->s_copy));
-      const int32_t* src = reinterpret_cast<const int32_t*>(w);
-      if (!e->pageable_access && e->E > 0) {
-        GX_TRY(dev_alloc(&sc.col_old, static_cast<size_t>(e->E)));
-        GX_CUDA(cudaMemcpyAsync(sc.col_old, w, sizeof(uint32_t) * e->E, cudaMemcpyHostToDevice, e->s_copy));
-        src = sc.col_old;
-      }
-      GX_TRY(relabel_scatter(e, src, reinterpret_cast<int32_t*>(e->d_w), false, sc.longs, sc.n_longs, sc.flag,
+      GX_TRY(dev_alloc(&sc.col_old, static_cast<size_t>(std::max<int64_t>(e->E, 1))));
+      GX_TRY(upload_async(e, sc.col_old, w, sizeof(uint32_t) * static_cast<size_t>(e->E), e->s_copy));
+      GX_TRY(relabel_scatter(e, sc.col_old, reinterpret_cast<int32_t*>(e->d_w), false, sc.longs, sc.n_longs, sc.flag,
                              e->s_copy));
     } else {
       GX_TRY(upload_async(e, e->d_w, w, sizeof(uint32_t) * static_cast<size_t>(e->E), e->s_copy));

@@ -1150,7 +1150,7 @@ static __global__ void relabel_order_kernel(const unsigned long long* sorted, un
 // v's list (src[off_old[v], off_old[v+1]), read in order, so the caller's
 // array is streamed once) goes to the new position off_new[perm[v]], with
 // every entry renamed through `rename` (source ids) or copied (rename null:
-// weights).  src may be host memory the device reads in place.  A warp per
+// weights).  A warp per
 // list of up to max_len entries; longer lists are appended to `longs` for
 // relabel_scatter_long_kernel.  Lists whose offsets leave [0, E] or decrease
 // are skipped (flag bit 0), and out-of-range ids are written as 0 (flag bit

@@ -93,9 +93,8 @@ typedef struct gx_config {
   int32_t relabel;             /* 1: a load without a shard-cache budget renumbers the vertices of each
                                   shard by descending in-degree, ties by id (each in-list keeps its
                                   order), so the pull kernel's tiles hold lists of like length and the
-                                  hot sources share cache lines.  The order is computed on the device
-                                  and the source ids are renamed as they are read from the caller's
-                                  array.  Every call still speaks the caller's numbering (values, start
+                                  hot sources share cache lines.  The order is computed and the source
+                                  ids renamed on the device, beside the upload.  Every call still speaks the caller's numbering (values, start
                                   values, sources, CC labels, weights, checkpoints, PPR rows);
                                   gx_batch_run and gx_get_device_graph refuse such an engine.  Ignored
                                   when E >= 2^32 or when bits(V) + bits(P) + 12 > 64.
