@@ -1147,51 +1147,66 @@ static __global__ void relabel_order_kernel(const unsigned long long* sorted, un
 }
 
 // Moves per-edge data from the caller's layout to the engine's: old vertex
-// v's list (src[off_old[v], off_old[v+1]), read in order, so the caller's
-// array is streamed once) goes to the new position off_new[perm[v]], with
-// every entry renamed through `rename` (source ids) or copied (rename null:
-// weights).  A warp per
-// list of up to max_len entries; longer lists are appended to `longs` for
-// relabel_scatter_long_kernel.  Lists whose offsets leave [0, E] or decrease
-// are skipped (flag bit 0), and out-of-range ids are written as 0 (flag bit
-// 1), so a malformed CSC neither reads nor writes out of bounds.
+// v's list (src[off_old[v], off_old[v+1])) goes to the new position
+// off_new[perm[v]], in order, with every entry renamed through `rename`
+// (source ids) or copied (rename null: weights).  A warp takes 32
+// consecutive old vertices: lists of up to 32 entries are walked by their
+// lane, the warp's longer ones (up to max_len) by the whole warp one after
+// another, and the longest are appended to `longs` for
+// relabel_scatter_long_kernel.  Lists whose offsets leave [0, E] or
+// decrease are skipped (flag bit 0) and out-of-range ids are written as 0
+// (flag bit 1), so a malformed CSC neither reads nor writes out of bounds.
+__device__ __forceinline__ int32_t relabel_entry(const int32_t* src, int64_t k, const int32_t* rename, int32_t V,
+                                                 unsigned int& f) {
+  int32_t x = src[k];
+  if (rename) {
+    if (x < 0 || x >= V) {
+      f |= 2u;
+      x = 0;
+    } else {
+      x = rename[x];
+    }
+  }
+  return x;
+}
 static __global__ void relabel_scatter_kernel(const int64_t* off_old, const int32_t* src, const int64_t* off_new,
                                               const int32_t* perm, const int32_t* rename, int32_t V, int64_t E,
                                               int64_t max_len, int32_t* dst, int32_t* longs,
                                               unsigned int longs_cap, unsigned int* n_longs, unsigned int* flag) {
   const int lane = threadIdx.x & 31;
-  const int warps = gridDim.x * (blockDim.x >> 5);
+  const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
   unsigned int f = 0;
-  for (int32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < V; v += warps) {
-    const int64_t b0 = off_old[v], e0 = off_old[v + 1];
-    if (b0 < 0 || e0 < b0 || e0 > E) {
-      f |= 1u;
-      continue;
-    }
-    const int64_t n = e0 - b0, b1 = off_new[perm[v]];
-    if (b1 < 0 || b1 + n > E) {
-      f |= 1u;
-      continue;
-    }
-    if (n > max_len) {
-      if (lane == 0) {
-        const unsigned int at = atomicAdd(n_longs, 1u);
-        if (at < longs_cap) longs[at] = v;
-        else f |= 1u;  // more long lists than E allows: overlapping lists
+  for (int64_t v0 = ((static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * 32; v0 < V;
+       v0 += warps * 32) {
+    const int64_t v = v0 + lane;
+    int64_t b0 = 0, n = 0, b1 = 0;
+    bool ok = false;
+    if (v < V) {
+      b0 = off_old[v];
+      const int64_t e0 = off_old[v + 1];
+      ok = b0 >= 0 && e0 >= b0 && e0 <= E;
+      if (ok) {
+        n = e0 - b0;
+        b1 = off_new[perm[v]];
+        ok = b1 >= 0 && b1 + n <= E;
       }
-      continue;
+      if (!ok) f |= 1u;
     }
-    for (int64_t j = lane; j < n; j += 32) {
-      int32_t x = src[b0 + j];
-      if (rename) {
-        if (x < 0 || x >= V) {
-          f |= 2u;
-          x = 0;
-        } else {
-          x = rename[x];
-        }
-      }
-      dst[b1 + j] = x;
+    if (ok && n <= 32) {
+      for (int64_t j = 0; j < n; ++j) dst[b1 + j] = relabel_entry(src, b0 + j, rename, V, f);
+    }
+    if (ok && n > max_len) {
+      const unsigned int at = atomicAdd(n_longs, 1u);
+      if (at < longs_cap) longs[at] = static_cast<int32_t>(v);
+      else f |= 1u;  // more long lists than E allows: overlapping lists
+    }
+    unsigned int mid = __ballot_sync(0xffffffffu, ok && n > 32 && n <= max_len);
+    while (mid) {
+      const int l = __ffs(mid) - 1;
+      mid &= mid - 1;
+      const int64_t mb0 = __shfl_sync(0xffffffffu, b0, l), mn = __shfl_sync(0xffffffffu, n, l);
+      const int64_t mb1 = __shfl_sync(0xffffffffu, b1, l);
+      for (int64_t j = lane; j < mn; j += 32) dst[mb1 + j] = relabel_entry(src, mb0 + j, rename, V, f);
     }
   }
   if (f) atomicOr(flag, f);
@@ -1205,18 +1220,7 @@ static __global__ void relabel_scatter_long_kernel(const int64_t* off_old, const
   for (unsigned int l = blockIdx.x; l < n_l; l += gridDim.x) {
     const int32_t v = longs[l];  // offsets checked by relabel_scatter_kernel
     const int64_t b0 = off_old[v], n = off_old[v + 1] - b0, b1 = off_new[perm[v]];
-    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) {
-      int32_t x = src[b0 + j];
-      if (rename) {
-        if (x < 0 || x >= V) {
-          f |= 2u;
-          x = 0;
-        } else {
-          x = rename[x];
-        }
-      }
-      dst[b1 + j] = x;
-    }
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) dst[b1 + j] = relabel_entry(src, b0 + j, rename, V, f);
   }
   if (f) atomicOr(flag, f);
 }
