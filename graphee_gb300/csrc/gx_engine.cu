@@ -261,10 +261,10 @@ gx_status relabel_scatter(gx_engine* e, const int32_t* src, int32_t* dst, bool r
                           unsigned int* n_longs, unsigned int* flag, cudaStream_t s) {
   const unsigned int cap = relabel_longs_cap(e->E);
   GX_CUDA(cudaMemsetAsync(n_longs, 0, sizeof(unsigned int), s));
-  relabel_scatter_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, src, e->d_off, e->d_perm,
+  relabel_scatter_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, src, e->d_off, e->d_inv,
                                                      rename ? e->d_perm : nullptr, e->V, e->E, kRelabelWarpMax, dst,
                                                      longs, cap, n_longs, flag);
-  relabel_scatter_long_kernel<<<e->n_sm * 2, 1024, 0, s>>>(e->d_off_old, src, e->d_off, e->d_perm,
+  relabel_scatter_long_kernel<<<e->n_sm * 2, 1024, 0, s>>>(e->d_off_old, src, e->d_off, e->d_inv,
                                                            rename ? e->d_perm : nullptr, e->V, dst, longs, cap,
                                                            n_longs, flag);
   GX_CUDA(cudaGetLastError());
@@ -317,11 +317,36 @@ __global__ void store_i64_kernel(int64_t* p, int64_t x) { *p = x; }
 // source ids, uploaded meanwhile, are then renamed into place in one pass
 // (still running on the copy stream when this returns; flag bits as
 // validate_csc_kernel's).  Also counts the dangling vertices.
+// Device-side phases of a load, for the verbose log: events recorded on a
+// stream, their times printed relative to the first once the stream is done.
+struct StreamMarks {
+  bool on = false;
+  std::vector<std::pair<const char*, cudaEvent_t>> ev;
+  void mark(const char* what, cudaStream_t s) {
+    if (!on) return;
+    cudaEvent_t x = nullptr;
+    if (cudaEventCreate(&x) != cudaSuccess) return;
+    cudaEventRecord(x, s);
+    ev.emplace_back(what, x);
+  }
+  ~StreamMarks() {
+    for (auto& m : ev) {
+      float ms = 0;
+      if (cudaEventSynchronize(m.second) == cudaSuccess) cudaEventElapsedTime(&ms, ev[0].second, m.second);
+      fprintf(stderr, "gx_load_csc device %-14s %8.2f ms\n", m.first, ms);
+    }
+    for (auto& m : ev) cudaEventDestroy(m.second);
+  }
+};
+
 gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, const int32_t* col,
                        const int32_t* outdeg, LoadScratch& sc) {
   const int32_t V = e->V, P = e->P;
   const int64_t E = e->E;
   cudaStream_t s = e->s_copy;
+  StreamMarks marks;
+  marks.on = e->cfg.verbose != 0;
+  marks.mark("start", s);
   const int vb = bits_for(V), pb = bits_for(P);
   GX_TRY(dev_alloc(&e->d_off, static_cast<size_t>(V) + 1));
   GX_TRY(dev_alloc(&e->d_col, static_cast<size_t>(E) + 8));
@@ -354,13 +379,16 @@ gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, 
   GX_TRY(dev_alloc(&sc.col_old, static_cast<size_t>(std::max<int64_t>(E, 1))));
   GX_TRY(upload_async(e, sc.col_old, col, sizeof(int32_t) * static_cast<size_t>(E), e->s_comp));
   GX_CUDA(cudaEventRecord(ev_col, e->s_comp));
+  marks.mark("ids uploaded", e->s_comp);
   GX_TRY(upload_async(e, e->d_off_old, off, sizeof(int64_t) * (static_cast<size_t>(V) + 1), s));
+  marks.mark("offsets", s);
   GX_CUDA(cudaMemcpyAsync(e->d_bounds, bounds, sizeof(int32_t) * (P + 1), cudaMemcpyHostToDevice, s));
   validate_csc_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, V, nullptr, E, sc.flag);
   relabel_keys_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, e->d_bounds, P, V, vb, sc.keys[0]);
   GX_CUDA(cudaGetLastError());
   unsigned long long* sorted = nullptr;
   GX_TRY(radix_sort_bits(sc.keys[0], sc.keys[1], V, vb, vb + 12 + pb, sc.hist, sc.offs, sc.part, s, &sorted));
+  marks.mark("sorted", s);
   // Out-degrees in the caller's numbering (while the device sorts).
   const int32_t* od = outdeg;
   if (!od) {
@@ -378,6 +406,7 @@ gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, 
   GX_CUDA(cudaGetLastError());
   GX_TRY(scan_u32(sc.len, V, reinterpret_cast<unsigned long long*>(e->d_off), sc.part, s));
   store_i64_kernel<<<1, 1, 0, s>>>(e->d_off + V, E);
+  marks.mark("new offsets", s);
   // The host's copies in the new numbering.
   host_resize_placed(e->off, static_cast<size_t>(V) + 1);
   host_resize_placed(e->outdeg, static_cast<size_t>(V));
@@ -389,8 +418,11 @@ gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, 
   GX_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   std::unique_ptr<CUevent_st, cudaError_t (*)(cudaEvent_t)> evg(ev, cudaEventDestroy);
   GX_CUDA(cudaEventRecord(ev, s));
+  marks.mark("host copies", s);
   GX_CUDA(cudaStreamWaitEvent(s, ev_col, 0));
+  marks.mark("ids ready", s);
   GX_TRY(relabel_scatter(e, sc.col_old, e->d_col, true, sc.longs, sc.n_longs, sc.flag, s));
+  marks.mark("ids renamed", s);
   GX_CUDA(cudaEventSynchronize(ev));
   return GX_OK;
 }

@@ -1146,13 +1146,14 @@ static __global__ void relabel_order_kernel(const unsigned long long* sorted, un
   }
 }
 
-// Moves per-edge data from the caller's layout to the engine's: old vertex
-// v's list (src[off_old[v], off_old[v+1])) goes to the new position
-// off_new[perm[v]], in order, with every entry renamed through `rename`
-// (source ids) or copied (rename null: weights).  A warp takes 32
-// consecutive old vertices: lists of up to 32 entries are walked by their
-// lane, the warp's longer ones (up to max_len) by the whole warp one after
-// another, and the longest are appended to `longs` for
+// Moves per-edge data from the caller's layout to the engine's: new vertex
+// i (old vertex inv[i]) gets the old list src[off_old[v], off_old[v+1]) at
+// off_new[i], in order, with every entry renamed through `rename` (source
+// ids) or copied (rename null: weights).  The new layout is written in
+// order (scattered list-sized writes cost far more than scattered reads).  A
+// warp takes 32 consecutive new vertices: lists of up to 32 entries are
+// walked by their lane, the warp's longer ones (up to max_len) by the whole
+// warp one after another, and the longest are appended to `longs` for
 // relabel_scatter_long_kernel.  Lists whose offsets leave [0, E] or
 // decrease are skipped (flag bit 0) and out-of-range ids are written as 0
 // (flag bit 1), so a malformed CSC neither reads nor writes out of bounds.
@@ -1170,24 +1171,25 @@ __device__ __forceinline__ int32_t relabel_entry(const int32_t* src, int64_t k, 
   return x;
 }
 static __global__ void relabel_scatter_kernel(const int64_t* off_old, const int32_t* src, const int64_t* off_new,
-                                              const int32_t* perm, const int32_t* rename, int32_t V, int64_t E,
+                                              const int32_t* inv, const int32_t* rename, int32_t V, int64_t E,
                                               int64_t max_len, int32_t* dst, int32_t* longs,
                                               unsigned int longs_cap, unsigned int* n_longs, unsigned int* flag) {
   const int lane = threadIdx.x & 31;
   const int64_t warps = static_cast<int64_t>(gridDim.x) * (blockDim.x >> 5);
   unsigned int f = 0;
-  for (int64_t v0 = ((static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * 32; v0 < V;
-       v0 += warps * 32) {
-    const int64_t v = v0 + lane;
+  for (int64_t i0 = ((static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * 32; i0 < V;
+       i0 += warps * 32) {
+    const int64_t i = i0 + lane;
     int64_t b0 = 0, n = 0, b1 = 0;
     bool ok = false;
-    if (v < V) {
+    if (i < V) {
+      const int32_t v = inv[i];
       b0 = off_old[v];
       const int64_t e0 = off_old[v + 1];
+      b1 = off_new[i];
       ok = b0 >= 0 && e0 >= b0 && e0 <= E;
       if (ok) {
         n = e0 - b0;
-        b1 = off_new[perm[v]];
         ok = b1 >= 0 && b1 + n <= E;
       }
       if (!ok) f |= 1u;
@@ -1197,7 +1199,7 @@ static __global__ void relabel_scatter_kernel(const int64_t* off_old, const int3
     }
     if (ok && n > max_len) {
       const unsigned int at = atomicAdd(n_longs, 1u);
-      if (at < longs_cap) longs[at] = static_cast<int32_t>(v);
+      if (at < longs_cap) longs[at] = static_cast<int32_t>(i);
       else f |= 1u;  // more long lists than E allows: overlapping lists
     }
     unsigned int mid = __ballot_sync(0xffffffffu, ok && n > 32 && n <= max_len);
@@ -1212,14 +1214,15 @@ static __global__ void relabel_scatter_kernel(const int64_t* off_old, const int3
   if (f) atomicOr(flag, f);
 }
 static __global__ void relabel_scatter_long_kernel(const int64_t* off_old, const int32_t* src, const int64_t* off_new,
-                                                   const int32_t* perm, const int32_t* rename, int32_t V,
+                                                   const int32_t* inv, const int32_t* rename, int32_t V,
                                                    int32_t* dst, const int32_t* longs, unsigned int longs_cap,
                                                    const unsigned int* n_longs, unsigned int* flag) {
   unsigned int f = 0;
   const unsigned int n_l = *n_longs < longs_cap ? *n_longs : longs_cap;
   for (unsigned int l = blockIdx.x; l < n_l; l += gridDim.x) {
-    const int32_t v = longs[l];  // offsets checked by relabel_scatter_kernel
-    const int64_t b0 = off_old[v], n = off_old[v + 1] - b0, b1 = off_new[perm[v]];
+    const int32_t i = longs[l];  // offsets checked by relabel_scatter_kernel
+    const int32_t v = inv[i];
+    const int64_t b0 = off_old[v], n = off_old[v + 1] - b0, b1 = off_new[i];
     for (int64_t j = threadIdx.x; j < n; j += blockDim.x) dst[b1 + j] = relabel_entry(src, b0 + j, rename, V, f);
   }
   if (f) atomicOr(flag, f);
