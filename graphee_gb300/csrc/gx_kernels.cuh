@@ -1149,14 +1149,15 @@ static __global__ void relabel_order_kernel(const unsigned long long* sorted, un
 // Moves per-edge data from the caller's layout to the engine's: new vertex
 // i (old vertex inv[i]) gets the old list src[off_old[v], off_old[v+1]) at
 // off_new[i], in order, with every entry renamed through `rename` (source
-// ids) or copied (rename null: weights).  The new layout is written in
-// order (scattered list-sized writes cost far more than scattered reads).  A
-// warp takes 32 consecutive new vertices: lists of up to 32 entries are
-// walked by their lane, the warp's longer ones (up to max_len) by the whole
-// warp one after another, and the longest are appended to `longs` for
-// relabel_scatter_long_kernel.  Lists whose offsets leave [0, E] or
-// decrease are skipped (flag bit 0) and out-of-range ids are written as 0
-// (flag bit 1), so a malformed CSC neither reads nor writes out of bounds.
+// ids) or copied (rename null: weights).  A warp takes 32 consecutive new
+// vertices, whose lists lie end to end in the new layout, and writes that
+// range 32 consecutive entries at a time (scattered list-sized writes cost
+// far more than the reads they save); each lane finds the list of its entry
+// among the warp's 32 start offsets by a binary search over the lanes.  Lists
+// longer than max_len are left to relabel_scatter_long_kernel (appended to
+// `longs`).  A warp whose lists have offsets that leave [0, E] or decrease
+// writes nothing (flag bit 0), and out-of-range ids are written as 0 (flag
+// bit 1), so a malformed CSC neither reads nor writes out of bounds.
 __device__ __forceinline__ int32_t relabel_entry(const int32_t* src, int64_t k, const int32_t* rename, int32_t V,
                                                  unsigned int& f) {
   int32_t x = src[k];
@@ -1180,35 +1181,43 @@ static __global__ void relabel_scatter_kernel(const int64_t* off_old, const int3
   for (int64_t i0 = ((static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * 32; i0 < V;
        i0 += warps * 32) {
     const int64_t i = i0 + lane;
-    int64_t b0 = 0, n = 0, b1 = 0;
-    bool ok = false;
+    int64_t b0 = 0, n = 0, b1 = INT64_MAX;  // lanes past V never hold an entry
+    bool ok = true;
     if (i < V) {
       const int32_t v = inv[i];
       b0 = off_old[v];
       const int64_t e0 = off_old[v + 1];
       b1 = off_new[i];
-      ok = b0 >= 0 && e0 >= b0 && e0 <= E;
-      if (ok) {
-        n = e0 - b0;
-        ok = b1 >= 0 && b1 + n <= E;
-      }
-      if (!ok) f |= 1u;
+      n = e0 - b0;
+      ok = b0 >= 0 && e0 >= b0 && e0 <= E && b1 >= 0 && b1 + n <= E;
     }
-    if (ok && n <= 32) {
-      for (int64_t j = 0; j < n; ++j) dst[b1 + j] = relabel_entry(src, b0 + j, rename, V, f);
+    // The warp's range in the new layout, and that its starts ascend.
+    const int64_t prev = __shfl_up_sync(0xffffffffu, b1 == INT64_MAX ? b1 : b1 + n, 1);
+    if (i < V && lane > 0 && prev != b1) ok = false;
+    if (__any_sync(0xffffffffu, !ok)) {
+      f |= 1u;
+      continue;
     }
-    if (ok && n > max_len) {
+    const bool is_long = i < V && n > max_len;
+    if (is_long) {
       const unsigned int at = atomicAdd(n_longs, 1u);
       if (at < longs_cap) longs[at] = static_cast<int32_t>(i);
       else f |= 1u;  // more long lists than E allows: overlapping lists
     }
-    unsigned int mid = __ballot_sync(0xffffffffu, ok && n > 32 && n <= max_len);
-    while (mid) {
-      const int l = __ffs(mid) - 1;
-      mid &= mid - 1;
-      const int64_t mb0 = __shfl_sync(0xffffffffu, b0, l), mn = __shfl_sync(0xffffffffu, n, l);
-      const int64_t mb1 = __shfl_sync(0xffffffffu, b1, l);
-      for (int64_t j = lane; j < mn; j += 32) dst[mb1 + j] = relabel_entry(src, mb0 + j, rename, V, f);
+    const int last = 31 - __clz(__ballot_sync(0xffffffffu, i < V));
+    const int64_t lo_p = __shfl_sync(0xffffffffu, b1, 0);
+    const int64_t hi_p = __shfl_sync(0xffffffffu, b1 + n, last);
+    for (int64_t p0 = lo_p; p0 < hi_p; p0 += 32) {
+      const int64_t p = p0 + lane;
+      int l = 0;  // the last lane whose list starts at or before p
+#pragma unroll
+      for (int step = 16; step > 0; step >>= 1) {
+        const int64_t b = __shfl_sync(0xffffffffu, b1, l + step);
+        if (b <= p) l += step;
+      }
+      const int64_t lb0 = __shfl_sync(0xffffffffu, b0, l), lb1 = __shfl_sync(0xffffffffu, b1, l);
+      const bool lskip = __shfl_sync(0xffffffffu, is_long, l);
+      if (p < hi_p && !lskip) dst[p] = relabel_entry(src, lb0 + (p - lb1), rename, V, f);
     }
   }
   if (f) atomicOr(flag, f);
