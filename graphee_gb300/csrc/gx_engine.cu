@@ -174,9 +174,9 @@ void build_units(gx_engine* e) {
   e->n_partials = n_part[P];
 }
 
-// Longest in-list a warp moves when the engine relabels; longer ones go to
-// the CTAs of relabel_scatter_long_kernel.
-constexpr int64_t kRelabelWarpMax = 65536;
+// Longest in-list that the warps of relabel_scatter_kernel move when the
+// engine relabels; longer ones go to the CTAs of relabel_scatter_long_kernel.
+constexpr int64_t kRelabelWarpMax = 512;
 
 // Values in the caller's numbering from the engine's buffer (d_stage).
 gx_status values_to_caller(gx_engine* e, const void* d_vals, cudaStream_t s) {
@@ -264,7 +264,7 @@ gx_status relabel_scatter(gx_engine* e, const int32_t* src, int32_t* dst, bool r
   relabel_scatter_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, src, e->d_off, e->d_inv,
                                                      rename ? e->d_perm : nullptr, e->V, e->E, kRelabelWarpMax, dst,
                                                      longs, cap, n_longs, flag);
-  relabel_scatter_long_kernel<<<e->n_sm * 2, 1024, 0, s>>>(e->d_off_old, src, e->d_off, e->d_inv,
+  relabel_scatter_long_kernel<<<e->n_sm * 4, 256, 0, s>>>(e->d_off_old, src, e->d_off, e->d_inv,
                                                            rename ? e->d_perm : nullptr, e->V, dst, longs, cap,
                                                            n_longs, flag);
   GX_CUDA(cudaGetLastError());

@@ -1150,26 +1150,22 @@ static __global__ void relabel_order_kernel(const unsigned long long* sorted, un
 // i (old vertex inv[i]) gets the old list src[off_old[v], off_old[v+1]) at
 // off_new[i], in order, with every entry renamed through `rename` (source
 // ids) or copied (rename null: weights).  A warp takes 32 consecutive new
-// vertices, whose lists lie end to end in the new layout, and writes that
-// range 32 consecutive entries at a time (scattered list-sized writes cost
-// far more than the reads they save); each lane finds the list of its entry
-// among the warp's 32 start offsets by a binary search over the lanes.  Lists
-// longer than max_len are left to relabel_scatter_long_kernel (appended to
-// `longs`).  A warp whose lists have offsets that leave [0, E] or decrease
-// writes nothing (flag bit 0), and out-of-range ids are written as 0 (flag
-// bit 1), so a malformed CSC neither reads nor writes out of bounds.
-__device__ __forceinline__ int32_t relabel_entry(const int32_t* src, int64_t k, const int32_t* rename, int32_t V,
-                                                 unsigned int& f) {
-  int32_t x = src[k];
-  if (rename) {
-    if (x < 0 || x >= V) {
-      f |= 2u;
-      x = 0;
-    } else {
-      x = rename[x];
-    }
+// vertices, whose lists lie end to end in the new layout, and moves their
+// entries 128 at a time, four per lane with the loads in flight together;
+// each lane finds the list of its entry by a binary search over the lanes'
+// running entry counts.  Lists longer than max_len go to `longs` for
+// relabel_scatter_long_kernel, so that no warp is left with a shard's
+// heaviest lists (the relabelling puts them side by side).  A warp whose
+// lists have offsets that leave [0, E] or decrease writes nothing (flag bit
+// 0), and out-of-range ids are written as 0 (flag bit 1), so a malformed CSC
+// neither reads nor writes out of bounds.
+__device__ __forceinline__ int32_t relabel_rename(int32_t x, const int32_t* rename, int32_t V, unsigned int& f) {
+  if (!rename) return x;
+  if (x < 0 || x >= V) {
+    f |= 2u;
+    return 0;
   }
-  return x;
+  return rename[x];
 }
 static __global__ void relabel_scatter_kernel(const int64_t* off_old, const int32_t* src, const int64_t* off_new,
                                               const int32_t* inv, const int32_t* rename, int32_t V, int64_t E,
@@ -1181,7 +1177,7 @@ static __global__ void relabel_scatter_kernel(const int64_t* off_old, const int3
   for (int64_t i0 = ((static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x) >> 5) * 32; i0 < V;
        i0 += warps * 32) {
     const int64_t i = i0 + lane;
-    int64_t b0 = 0, n = 0, b1 = INT64_MAX;  // lanes past V never hold an entry
+    int64_t b0 = 0, n = 0, b1 = 0;
     bool ok = true;
     if (i < V) {
       const int32_t v = inv[i];
@@ -1191,37 +1187,52 @@ static __global__ void relabel_scatter_kernel(const int64_t* off_old, const int3
       n = e0 - b0;
       ok = b0 >= 0 && e0 >= b0 && e0 <= E && b1 >= 0 && b1 + n <= E;
     }
-    // The warp's range in the new layout, and that its starts ascend.
-    const int64_t prev = __shfl_up_sync(0xffffffffu, b1 == INT64_MAX ? b1 : b1 + n, 1);
-    if (i < V && lane > 0 && prev != b1) ok = false;
     if (__any_sync(0xffffffffu, !ok)) {
       f |= 1u;
       continue;
     }
-    const bool is_long = i < V && n > max_len;
-    if (is_long) {
+    if (n > max_len) {
       const unsigned int at = atomicAdd(n_longs, 1u);
       if (at < longs_cap) longs[at] = static_cast<int32_t>(i);
       else f |= 1u;  // more long lists than E allows: overlapping lists
     }
-    const int last = 31 - __clz(__ballot_sync(0xffffffffu, i < V));
-    const int64_t lo_p = __shfl_sync(0xffffffffu, b1, 0);
-    const int64_t hi_p = __shfl_sync(0xffffffffu, b1 + n, last);
-    for (int64_t p0 = lo_p; p0 < hi_p; p0 += 32) {
-      const int64_t p = p0 + lane;
-      int l = 0;  // the last lane whose list starts at or before p
+    const int64_t eff = n > max_len ? 0 : n;
+    int64_t pre = eff;  // inclusive scan over the lanes, then exclusive
 #pragma unroll
-      for (int step = 16; step > 0; step >>= 1) {
-        const int64_t b = __shfl_sync(0xffffffffu, b1, l + step);
-        if (b <= p) l += step;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t t = __shfl_up_sync(0xffffffffu, pre, o);
+      if (lane >= o) pre += t;
+    }
+    const int64_t tot = __shfl_sync(0xffffffffu, pre, 31);
+    pre -= eff;
+    for (int64_t q0 = 0; q0 < tot; q0 += 128) {
+      int64_t sk[4], dk[4];
+      int32_t x[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t q = q0 + 32 * u + lane;
+        int l = 0;  // the last lane whose entries start at or before q
+#pragma unroll
+        for (int step = 16; step > 0; step >>= 1) {
+          const int64_t b = __shfl_sync(0xffffffffu, pre, l + step);
+          if (b <= q) l += step;
+        }
+        const int64_t lp = __shfl_sync(0xffffffffu, pre, l);
+        sk[u] = __shfl_sync(0xffffffffu, b0, l) + (q - lp);
+        dk[u] = q < tot ? __shfl_sync(0xffffffffu, b1, l) + (q - lp) : -1;
       }
-      const int64_t lb0 = __shfl_sync(0xffffffffu, b0, l), lb1 = __shfl_sync(0xffffffffu, b1, l);
-      const bool lskip = __shfl_sync(0xffffffffu, is_long, l);
-      if (p < hi_p && !lskip) dst[p] = relabel_entry(src, lb0 + (p - lb1), rename, V, f);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) x[u] = dk[u] >= 0 ? src[sk[u]] : 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) x[u] = dk[u] >= 0 ? relabel_rename(x[u], rename, V, f) : 0;
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (dk[u] >= 0) dst[dk[u]] = x[u];
     }
   }
   if (f) atomicOr(flag, f);
 }
+// A CTA per long list, four entries per thread in flight.
 static __global__ void relabel_scatter_long_kernel(const int64_t* off_old, const int32_t* src, const int64_t* off_new,
                                                    const int32_t* inv, const int32_t* rename, int32_t V,
                                                    int32_t* dst, const int32_t* longs, unsigned int longs_cap,
@@ -1232,10 +1243,29 @@ static __global__ void relabel_scatter_long_kernel(const int64_t* off_old, const
     const int32_t i = longs[l];  // offsets checked by relabel_scatter_kernel
     const int32_t v = inv[i];
     const int64_t b0 = off_old[v], n = off_old[v + 1] - b0, b1 = off_new[i];
-    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) dst[b1 + j] = relabel_entry(src, b0 + j, rename, V, f);
+    const int64_t span = 4 * static_cast<int64_t>(blockDim.x);
+    for (int64_t j0 = 0; j0 < n; j0 += span) {
+      int32_t x[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t j = j0 + u * blockDim.x + threadIdx.x;
+        x[u] = j < n ? src[b0 + j] : 0;
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t j = j0 + u * blockDim.x + threadIdx.x;
+        if (j < n) x[u] = relabel_rename(x[u], rename, V, f);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int64_t j = j0 + u * blockDim.x + threadIdx.x;
+        if (j < n) dst[b1 + j] = x[u];
+      }
+    }
   }
   if (f) atomicOr(flag, f);
 }
+
 // out[v] = in[perm[v]] (values to the caller's numbering), and the inverse.
 static __global__ void gather_values_kernel(const uint32_t* in, const int32_t* perm, int32_t V, uint32_t* out) {
   for (int32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) out[v] = in[perm[v]];
