@@ -1217,9 +1217,12 @@ static __global__ void relabel_scatter_kernel(const int64_t* off_old, const int3
           const int64_t b = __shfl_sync(0xffffffffu, pre, l + step);
           if (b <= q) l += step;
         }
+        // (every lane takes part in every shuffle)
         const int64_t lp = __shfl_sync(0xffffffffu, pre, l);
-        sk[u] = __shfl_sync(0xffffffffu, b0, l) + (q - lp);
-        dk[u] = q < tot ? __shfl_sync(0xffffffffu, b1, l) + (q - lp) : -1;
+        const int64_t lb0 = __shfl_sync(0xffffffffu, b0, l);
+        const int64_t lb1 = __shfl_sync(0xffffffffu, b1, l);
+        sk[u] = lb0 + (q - lp);
+        dk[u] = q < tot ? lb1 + (q - lp) : -1;
       }
 #pragma unroll
       for (int u = 0; u < 4; ++u) x[u] = dk[u] >= 0 ? src[sk[u]] : 0;
