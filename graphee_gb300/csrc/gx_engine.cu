@@ -215,10 +215,11 @@ __global__ void host_copy_kernel(const void* __restrict__ src, void* __restrict_
 // Host-to-device copy of a caller's array on `s`: read in place by a kernel
 // when the device can (no staging through pinned buffers, and the host thread
 // is free at once), else cudaMemcpyAsync.
-gx_status upload_async(gx_engine* e, void* dst, const void* src, size_t bytes, cudaStream_t s) {
+gx_status upload_async(gx_engine* e, void* dst, const void* src, size_t bytes, cudaStream_t s,
+                       int blocks_per_sm = 8) {
   if (bytes == 0) return GX_OK;
   if (e->pageable_access && (reinterpret_cast<uintptr_t>(src) & 3u) == 0 && bytes % 4 == 0) {
-    host_copy_kernel<<<e->n_sm * 8, 256, 0, s>>>(src, dst, bytes);
+    host_copy_kernel<<<e->n_sm * blocks_per_sm, 256, 0, s>>>(src, dst, bytes);
     GX_CUDA(cudaGetLastError());
   } else {
     GX_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
@@ -384,7 +385,9 @@ gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, 
   marks.mark("offsets", s);
   GX_TRY(dev_alloc(&sc.col_old, static_cast<size_t>(std::max<int64_t>(E, 1))));
   GX_CUDA(cudaStreamWaitEvent(e->s_comp, ev_off, 0));
-  GX_TRY(upload_async(e, sc.col_old, col, sizeof(int32_t) * static_cast<size_t>(E), e->s_comp));
+  // (two copy blocks per SM keep the host link busy and leave the SMs to
+  // the ordering kernels)
+  GX_TRY(upload_async(e, sc.col_old, col, sizeof(int32_t) * static_cast<size_t>(E), e->s_comp, 2));
   GX_CUDA(cudaEventRecord(ev_col, e->s_comp));
   marks.mark("ids uploaded", e->s_comp);
   GX_CUDA(cudaMemcpyAsync(e->d_bounds, bounds, sizeof(int32_t) * (P + 1), cudaMemcpyHostToDevice, s));
