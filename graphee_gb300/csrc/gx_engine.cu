@@ -381,6 +381,7 @@ gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, 
   GX_CUDA(cudaEventCreateWithFlags(&ev_col, cudaEventDisableTiming));
   std::unique_ptr<CUevent_st, cudaError_t (*)(cudaEvent_t)> ev_col_g(ev_col, cudaEventDestroy);
   GX_TRY(upload_async(e, e->d_off_old, off, sizeof(int64_t) * (static_cast<size_t>(V) + 1), s));
+  GX_TRY(upload_async(e, e->d_bounds, bounds, sizeof(int32_t) * (static_cast<size_t>(P) + 1), s));
   GX_CUDA(cudaEventRecord(ev_off, s));
   marks.mark("offsets", s);
   GX_TRY(dev_alloc(&sc.col_old, static_cast<size_t>(std::max<int64_t>(E, 1))));
@@ -390,10 +391,10 @@ gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, 
   GX_TRY(upload_async(e, sc.col_old, col, sizeof(int32_t) * static_cast<size_t>(E), e->s_comp, 2));
   GX_CUDA(cudaEventRecord(ev_col, e->s_comp));
   marks.mark("ids uploaded", e->s_comp);
-  GX_CUDA(cudaMemcpyAsync(e->d_bounds, bounds, sizeof(int32_t) * (P + 1), cudaMemcpyHostToDevice, s));
   validate_csc_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, V, nullptr, E, sc.flag);
   relabel_keys_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, e->d_bounds, P, V, vb, sc.keys[0]);
   GX_CUDA(cudaGetLastError());
+  marks.mark("keys", s);
   unsigned long long* sorted = nullptr;
   GX_TRY(radix_sort_bits(sc.keys[0], sc.keys[1], V, vb, vb + 12 + pb, sc.hist, sc.offs, sc.part, s, &sorted));
   marks.mark("sorted", s);
