@@ -71,7 +71,10 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--no-sssp", action="store_true", help="skip the SSSP keys of the default run")
     ap.add_argument("--no-scale24", action="store_true", help="skip the scale-24 keys of the default run")
-    ap.add_argument("--no-relabel", action="store_true", help="skip the relabelled-layout keys of the default run")
+    ap.add_argument("--layout", default="relabel", choices=["relabel", "plain"],
+                    help="the headline engine's vertex layout: relabel = config.relabel (per-shard renumbering "
+                         "by in-degree at load), plain = the caller's numbering")
+    ap.add_argument("--no-other-layout", action="store_true", help="skip the keys of the other layout")
     ap.add_argument("--workload", default="pagerank",
                     choices=["pagerank", "cc_tc", "stream", "batch", "ppr", "warm"],
                     help="pagerank = the headline run; the others measure the remaining configurations")
@@ -174,9 +177,14 @@ def measured_peak_hbm():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(workload: str):
+def layout_cfg(layout: str) -> dict:
+    return {"relabel": 1} if layout == "relabel" else {}
+
+
+def ncu_traffic(workload: str, layout: str = "plain"):
     """DRAM bytes per pull launch from the committed ncu summary, if any."""
-    p = ROOT / "profiles" / f"pull_kernel_pagerank_ref_{workload}.md"
+    tag = "relabel_" if layout == "relabel" else ""
+    p = ROOT / "profiles" / f"pull_kernel_pagerank_ref_{tag}{workload}.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
@@ -335,7 +343,8 @@ def run_gx(args, rank, local_rank, world):
         torch.cuda.synchronize()
 
     g, build_s = build_graph(args, device=local_rank)
-    eng = gx.Engine(device=local_rank)
+    lcfg = layout_cfg(args.layout)
+    eng = gx.Engine(device=local_rank, **lcfg)
     eng.load(g)
     clk = ClockSampler(local_rank).__enter__()
     for _ in range(args.warmup):
@@ -359,11 +368,11 @@ def run_gx(args, rank, local_rank, world):
     value = eps / 1e9
 
     # Dominant kernel, timed live with CUDA events on the engine's stream.
-    pull_ms = pull_kernel_ms(gx, g, local_rank, args.iters)
+    pull_ms = pull_kernel_ms(gx, g, local_rank, args.iters, **lcfg)
     alg_bytes = 8 * g.E + 24 * g.V
     peak, peak_kind = measured_peak_hbm()
     achieved = alg_bytes / (pull_ms / 1000) / 1e9
-    traffic = ncu_traffic(workload_name(args))
+    traffic = ncu_traffic(workload_name(args), args.layout)
 
     # End to end through the C ABI: host buffers in, values out, every step.
     # One engine serves every step (created before the timed steps); each step
@@ -371,7 +380,7 @@ def run_gx(args, rank, local_rank, world):
     # reads the ranks back into the caller's result buffer.
     e2e_s = []
     result = np.empty(g.V, np.float32)
-    e2 = gx.Engine(device=local_rank)
+    e2 = gx.Engine(device=local_rank, **lcfg)
     for i in range(args.e2e_steps + 1):
         barrier()
         with clk.window() if i > 0 else _nullcontext():
@@ -391,35 +400,38 @@ def run_gx(args, rank, local_rank, world):
     d2h = 4 * g.V
     assert np.isfinite(vals).all()
 
-    # The relabelled layout (config.relabel: per-shard renumbering by
-    # descending in-degree at load): device steps, the pull kernel, and the
-    # same end-to-end step, whose load now includes the renumbering.
-    relabel = None
-    if not args.no_relabel:
-        with gx.Engine(device=local_rank, relabel=1) as er:
-            er.load(g)
+    # The other vertex layout (config.relabel on or off): device steps, the
+    # pull kernel and the same end-to-end step (a relabelling load includes
+    # the renumbering).
+    other = None
+    other_name = "plain" if args.layout == "relabel" else "relabel"
+    if not args.no_other_layout:
+        ocfg = layout_cfg(other_name)
+        with gx.Engine(device=local_rank, **ocfg) as eo:
+            eo.load(g)
             for _ in range(args.warmup):
-                er.run(gx.APP_PAGERANK_REF, args.iters)
-            runs_r = [er.run(gx.APP_PAGERANK_REF, args.iters) for _ in range(args.steps)]
-            launches += sum(r["kernel_launches"] for r in runs_r)
-            ms_r = sum(r["ms_total"] for r in runs_r) / len(runs_r)
-            e2e_r = []
-            for i in range(3):
+                eo.run(gx.APP_PAGERANK_REF, args.iters)
+            runs_o = [eo.run(gx.APP_PAGERANK_REF, args.iters) for _ in range(args.steps)]
+            launches += sum(r["kernel_launches"] for r in runs_o)
+            ms_o = sum(r["ms_total"] for r in runs_o) / len(runs_o)
+            e2e_o = []
+            for i in range(args.e2e_steps + 1):
                 torch.cuda.synchronize()
                 t1 = time.perf_counter()
-                er.load(g)
-                er.run(gx.APP_PAGERANK_REF, args.iters)
-                er.values(out=result)
+                eo.load(g)
+                eo.run(gx.APP_PAGERANK_REF, args.iters)
+                eo.values(out=result)
                 torch.cuda.synchronize()
                 if i > 0:
-                    e2e_r.append(time.perf_counter() - t1)
+                    e2e_o.append(time.perf_counter() - t1)
             assert np.isfinite(result).all()
-        kr = pull_kernel_ms(gx, g, local_rank, args.iters, relabel=1)
-        relabel = {"value": g.E * args.iters / (ms_r / 1000) / 1e9, "unit": "GTEPS", "ms_per_step": ms_r,
-                   "kernel_ms": kr, "achieved_gbs": alg_bytes / (kr / 1000) / 1e9,
-                   "frac": alg_bytes / (kr / 1000) / 1e9 / peak,
-                   "e2e": {"value": edges_per_step / (sum(e2e_r) / len(e2e_r)) / 1e9, "unit": "GTEPS",
-                           "s_per_step": sum(e2e_r) / len(e2e_r), "steps": len(e2e_r)}}
+        ko = pull_kernel_ms(gx, g, local_rank, args.iters, **ocfg)
+        other = {"value": g.E * args.iters / (ms_o / 1000) / 1e9, "unit": "GTEPS", "ms_per_step": ms_o,
+                 "kernel_ms": ko, "achieved_gbs": alg_bytes / (ko / 1000) / 1e9,
+                 "frac": alg_bytes / (ko / 1000) / 1e9 / peak,
+                 "traffic": ncu_traffic(workload_name(args), other_name),
+                 "e2e": {"value": edges_per_step / (sum(e2e_o) / len(e2e_o)) / 1e9, "unit": "GTEPS",
+                         "s_per_step": sum(e2e_o) / len(e2e_o), "steps": len(e2e_o)}}
 
     sssp = None
     if not args.no_sssp:
@@ -440,7 +452,7 @@ def run_gx(args, rank, local_rank, world):
         # scanned; algorithmic bytes 12 per edge (index, weight, distance
         # gather) + 16 per vertex of the swept shards (offsets, old and new
         # distance), the latter prorated by the edges a selective step swept.
-        pe = gx.Engine(device=local_rank, profile=1)
+        pe = gx.Engine(device=local_rank, profile=1, **lcfg)
         pe.load(g)
         pe.set_weights(g.weights)
         pe.run(gx.APP_SSSP, 10000, source=0, weighted=True)
@@ -461,14 +473,14 @@ def run_gx(args, rank, local_rank, world):
     rmat24 = None
     if args.scale == 26 and not args.no_scale24:
         g24 = gx.rmat_graph(24, args.edge_factor, seed=SEED, P=SHARDS, gpu=True, device=local_rank)
-        with gx.Engine(device=local_rank) as e24:
+        with gx.Engine(device=local_rank, **lcfg) as e24:
             e24.load(g24)
             for _ in range(args.warmup):
                 e24.run(gx.APP_PAGERANK_REF, args.iters)
             runs24 = [e24.run(gx.APP_PAGERANK_REF, args.iters) for _ in range(args.steps)]
         launches += sum(r["kernel_launches"] for r in runs24)
         ms24 = sum(r["ms_total"] for r in runs24) / len(runs24)
-        k24 = pull_kernel_ms(gx, g24, local_rank, args.iters)
+        k24 = pull_kernel_ms(gx, g24, local_rank, args.iters, **lcfg)
         b24 = 8 * g24.E + 24 * g24.V
         rmat24 = {"value": g24.E * args.iters / (ms24 / 1000) / 1e9, "unit": "GTEPS", "ms_per_step": ms24,
                   "vertices": g24.V, "edges": g24.E, "kernel_ms": k24,
@@ -493,14 +505,17 @@ def run_gx(args, rank, local_rank, world):
                 "e2e": {"value": e2e_eps / 1e9, "unit": "GTEPS",
                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "s_per_step": e2e_step,
                         "step": "gx_load_csc from host arrays + gx_run (20 supersteps) + gx_get_values into a "
-                                "reused host buffer, one engine"},
+                                "reused host buffer, one engine" +
+                                (" with config.relabel = 1 (the renumbering is part of every load)"
+                                 if args.layout == "relabel" else "")},
                 "gpu_launches": launches,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": traffic, "peak_source": peak_kind,
                              "kernel": "pull_kernel<PAGERANK_REF>", "kernel_ms": pull_ms,
                              "algorithmic_bytes_per_launch": alg_bytes},
                 "cpu_baseline": cpu, "clocks": clocks, "wall_s_timed": wall, "sssp": sssp,
-                "rmat24": rmat24, "relabel": relabel, "iterations_per_step": iters_done / args.steps}
+                "rmat24": rmat24, "layout": args.layout, other_name: other,
+                "iterations_per_step": iters_done / args.steps}
         print(json.dumps(line), flush=True)
     eng.close()
     if dist is not None:

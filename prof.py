@@ -60,14 +60,15 @@ def main():
     ap.add_argument("--heavy-degree", type=int, default=None)
     ap.add_argument("--tile-edges", type=int, default=None)
     ap.add_argument("--profile-kernels", type=int, default=0, help="time each pull launch with CUDA events")
+    ap.add_argument("--relabel", type=int, default=0, help="config.relabel: per-shard renumbering at load")
     a = ap.parse_args()
     if a.app in OTHER:
         run_other(a)
         return
     sym = a.app == "cc"
     g = gx.rmat_graph(a.scale, a.edge_factor, seed=20240601, P=256, symmetric=sym,
-                      weight_seed=7 if a.app == "sssp" else None)
-    cfg = {"use_graph": a.graph, "profile": a.profile_kernels}
+                      weight_seed=7 if a.app == "sssp" else None, gpu=True)
+    cfg = {"use_graph": a.graph, "profile": a.profile_kernels, "relabel": a.relabel}
     if a.heavy_degree is not None:
         cfg["heavy_degree"] = a.heavy_degree
     if a.tile_edges is not None:
