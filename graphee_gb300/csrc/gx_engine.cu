@@ -371,26 +371,21 @@ gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, 
   GX_TRY(dev_alloc(&sc.flag, 1));
   GX_CUDA(cudaMemsetAsync(sc.flag, 0, sizeof(unsigned int), s));
   GX_CUDA(cudaMemsetAsync(e->d_col + E, 0, 8 * sizeof(int32_t), s));
-  // The offsets go up first; then the caller's source ids go up on the
-  // compute stream (idle during a load) while the copy stream works out the
-  // order (a device pass that read the ids in place list by list would take
-  // small, latency-bound host reads).
-  cudaEvent_t ev_off = nullptr, ev_col = nullptr;
-  GX_CUDA(cudaEventCreateWithFlags(&ev_off, cudaEventDisableTiming));
-  std::unique_ptr<CUevent_st, cudaError_t (*)(cudaEvent_t)> ev_off_g(ev_off, cudaEventDestroy);
+  // The offsets go up first and the device works out the order; then the
+  // caller's source ids go up on the compute stream (idle during a load)
+  // while the new offsets, out-degrees and permutation come back to the
+  // host.  (Reading the ids in place list by list would take small,
+  // latency-bound host reads; an upload beside the sort slows the sort
+  // several times over.)
+  cudaEvent_t ev_order = nullptr, ev_col = nullptr;
+  GX_CUDA(cudaEventCreateWithFlags(&ev_order, cudaEventDisableTiming));
+  std::unique_ptr<CUevent_st, cudaError_t (*)(cudaEvent_t)> ev_order_g(ev_order, cudaEventDestroy);
   GX_CUDA(cudaEventCreateWithFlags(&ev_col, cudaEventDisableTiming));
   std::unique_ptr<CUevent_st, cudaError_t (*)(cudaEvent_t)> ev_col_g(ev_col, cudaEventDestroy);
+  GX_TRY(dev_alloc(&sc.col_old, static_cast<size_t>(std::max<int64_t>(E, 1))));
   GX_TRY(upload_async(e, e->d_off_old, off, sizeof(int64_t) * (static_cast<size_t>(V) + 1), s));
   GX_TRY(upload_async(e, e->d_bounds, bounds, sizeof(int32_t) * (static_cast<size_t>(P) + 1), s));
-  GX_CUDA(cudaEventRecord(ev_off, s));
   marks.mark("offsets", s);
-  GX_TRY(dev_alloc(&sc.col_old, static_cast<size_t>(std::max<int64_t>(E, 1))));
-  GX_CUDA(cudaStreamWaitEvent(e->s_comp, ev_off, 0));
-  // (two copy blocks per SM keep the host link busy and leave the SMs to
-  // the ordering kernels)
-  GX_TRY(upload_async(e, sc.col_old, col, sizeof(int32_t) * static_cast<size_t>(E), e->s_comp, 2));
-  GX_CUDA(cudaEventRecord(ev_col, e->s_comp));
-  marks.mark("ids uploaded", e->s_comp);
   validate_csc_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, V, nullptr, E, sc.flag);
   relabel_keys_kernel<<<e->n_sm * 8, 256, 0, s>>>(e->d_off_old, e->d_bounds, P, V, vb, sc.keys[0]);
   GX_CUDA(cudaGetLastError());
@@ -415,7 +410,12 @@ gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, 
   GX_CUDA(cudaGetLastError());
   GX_TRY(scan_u32(sc.len, V, reinterpret_cast<unsigned long long*>(e->d_off), sc.part, s));
   store_i64_kernel<<<1, 1, 0, s>>>(e->d_off + V, E);
+  GX_CUDA(cudaEventRecord(ev_order, s));
   marks.mark("new offsets", s);
+  GX_CUDA(cudaStreamWaitEvent(e->s_comp, ev_order, 0));
+  GX_TRY(upload_async(e, sc.col_old, col, sizeof(int32_t) * static_cast<size_t>(E), e->s_comp));
+  GX_CUDA(cudaEventRecord(ev_col, e->s_comp));
+  marks.mark("ids uploaded", e->s_comp);
   // The host's copies in the new numbering.
   host_resize_placed(e->off, static_cast<size_t>(V) + 1);
   host_resize_placed(e->outdeg, static_cast<size_t>(V));
