@@ -425,16 +425,17 @@ def test_selective_steps_sweep_exactly_the_marked_shards(budget):
     assert checked > L // 2
 
 
-@pytest.mark.parametrize("budget", [-1, 0])
-def test_graph_without_edges(budget):
+@pytest.mark.parametrize("budget,relabel", [(-1, 0), (0, 0), (-1, 1)])
+def test_graph_without_edges(budget, relabel):
     """No edges at all (every shard empty): the apps still follow the
-    reference's loop and stop rule, resident or with a zero budget."""
+    reference's loop and stop rule, resident, relabelled or with a zero
+    budget."""
     V, P = 100, 4
     g = gx.Graph(V, np.zeros(V + 1, np.int64), np.zeros(0, np.int32), None, P)
     for app, kw, oapp in [(gx.APP_PAGERANK_REF, {}, O.PAGERANK_REF), (gx.APP_SSSP, {"source": 0}, O.SSSP),
                           (gx.APP_CC, {}, O.CC)]:
         ref, ch, _ = O.run(oapp, V, P, g.bounds, g.off, g.col, g.outdeg, 50, **kw)
-        with gx.Engine(cache_budget_bytes=budget) as e:
+        with gx.Engine(cache_budget_bytes=budget, relabel=relabel) as e:
             e.load(g)
             st = e.run(app, 50, **kw)
             assert np.array_equal(e.values().view(np.uint32), ref.view(np.uint32)), app
