@@ -872,33 +872,51 @@ __global__ void __launch_bounds__(kThreads) push_kernel(PushArgs a) {
     const int total = __shfl_sync(0xffffffffu, incl, 31);
     const int excl = incl - d;
     la.edges += static_cast<unsigned long long>(d);
-    for (int k0 = 0; k0 < total; k0 += 32) {
-      const int k = k0 + lane;
-      // Largest j with excl[j] <= k; that entry has d[j] > 0 when k < total.
-      int j = 0;
+    // 128 edges per round, four per lane, each stage's loads in flight
+    // together (index and weight, then the destination's value); the value
+    // read is only a filter before the atomicMin, so a stale one is harmless.
+    for (int k0 = 0; k0 < total; k0 += 128) {
+      long long edge[4];
+      uint32_t sv[4];
+      bool ok[4];
 #pragma unroll
-      for (int sp = 16; sp > 0; sp >>= 1) {
-        const int ex = __shfl_sync(0xffffffffu, excl, j + sp);
-        if (ex <= k) j += sp;
+      for (int u = 0; u < 4; ++u) {
+        const int k = k0 + 32 * u + lane;
+        // Largest j with excl[j] <= k; that entry has d[j] > 0 when k < total.
+        // (every lane takes part in every shuffle)
+        int j = 0;
+#pragma unroll
+        for (int sp = 16; sp > 0; sp >>= 1) {
+          const int ex = __shfl_sync(0xffffffffu, excl, j + sp);
+          if (ex <= k) j += sp;
+        }
+        const int exj = __shfl_sync(0xffffffffu, excl, j);
+        const long long bj = __shfl_sync(0xffffffffu, b, j);
+        sv[u] = __shfl_sync(0xffffffffu, su, j);
+        ok[u] = k < total;
+        edge[u] = bj + (k - exj);
       }
-      const int exj = __shfl_sync(0xffffffffu, excl, j);
-      const long long bj = __shfl_sync(0xffffffffu, b, j);
-      const uint32_t sj = __shfl_sync(0xffffffffu, su, j);
-      if (k < total) {
-        const long long edge = bj + (k - exj);
-        const int vtx = __ldcs(a.ocol + edge);
-        T cand;
-        if constexpr (APP == K_SSSP_UNIT) cand = static_cast<T>(sj) + 1;
-        else if constexpr (APP == K_SSSP_W) cand = sat_add(sj, __ldcs(a.ow + edge));
-        else cand = static_cast<T>(sj);
-        if (cand < val[vtx]) {
-          const T prev = atomicMin(val + vtx, cand);
-          if (cand < prev) {
-            const uint32_t bit = 1u << (vtx & 31);
-            const uint32_t was = atomicOr(a.bm + (vtx >> 5), bit);
+      int vtx[4];
+      T cand[4], now[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        vtx[u] = ok[u] ? __ldcs(a.ocol + edge[u]) : 0;
+        if constexpr (APP == K_SSSP_UNIT) cand[u] = static_cast<T>(sv[u]) + 1;
+        else if constexpr (APP == K_SSSP_W) cand[u] = sat_add(sv[u], ok[u] ? __ldcs(a.ow + edge[u]) : 0u);
+        else cand[u] = static_cast<T>(sv[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) now[u] = ok[u] ? val[vtx[u]] : cand[u];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        if (ok[u] && cand[u] < now[u]) {
+          const T prev = atomicMin(val + vtx[u], cand[u]);
+          if (cand[u] < prev) {
+            const uint32_t bit = 1u << (vtx[u] & 31);
+            const uint32_t was = atomicOr(a.bm + (vtx[u] >> 5), bit);
             if (!(was & bit)) {
               la.changed += 1;
-              la.fedges += static_cast<unsigned long long>(__ldg(a.outdeg + vtx));
+              la.fedges += static_cast<unsigned long long>(__ldg(a.outdeg + vtx[u]));
             }
           }
         }
