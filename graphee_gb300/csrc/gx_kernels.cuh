@@ -997,32 +997,32 @@ __global__ void __launch_bounds__(kThreads) finalize_kernel(FinArgs a) {
       }
     }
     if (push_next) {
-      // The warp takes its 32 words one at a time, a lane per vertex (the
-      // out-degree and value loads of a word are then coalesced), and
-      // reserves each word's entries with one atomic.
-      for (int j = 0; j < 32; ++j) {
-        const uint32_t wj = __shfl_sync(0xffffffffu, word, j);
-        if (wj == 0) continue;  // warp-uniform
-        const int u = ((w0 + j) << 5) + lane;
-        const bool set = (wj >> lane) & 1u;
-        const int od = set ? __ldg(a.outdeg + u) : 0;
-        const unsigned n_ent = static_cast<unsigned>((od + kPushChunk - 1) / kPushChunk);  // sinks need no entry
-        T vu = set ? newv[u] : T(0);
-        unsigned incl = n_ent;
+      unsigned n_ent = 0;
+      for (uint32_t x = word; x; x &= x - 1) {
+        const int od = __ldg(a.outdeg + (w << 5) + __ffs(x) - 1);
+        n_ent += static_cast<unsigned>((od + kPushChunk - 1) / kPushChunk);  // sinks need no entry
+      }
+      unsigned incl = n_ent;
 #pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
-          if (lane >= o) incl += t;
-        }
-        const unsigned tot = __shfl_sync(0xffffffffu, incl, 31);
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      const unsigned tot = __shfl_sync(0xffffffffu, incl, 31);
+      if (tot) {
         unsigned wbase = 0;
-        if (lane == 31 && tot) wbase = atomicAdd(&ctl->next_frontier, tot);
+        if (lane == 31) wbase = atomicAdd(&ctl->next_frontier, tot);
         wbase = __shfl_sync(0xffffffffu, wbase, 31);
         unsigned long long pos = static_cast<unsigned long long>(wbase) + (incl - n_ent);
-        const int bits = *reinterpret_cast<int*>(&vu);
-        for (int k = 0; k < od; k += kPushChunk, ++pos) {
-          if (pos < a.frontier_cap) a.frontier[pos] = make_int4(u, bits, k, 0);
-          else ctl->error = 2;
+        for (uint32_t x = word; x; x &= x - 1) {
+          const int u = (w << 5) + __ffs(x) - 1;
+          const int od = __ldg(a.outdeg + u);
+          T vu = newv[u];
+          const int bits = *reinterpret_cast<int*>(&vu);
+          for (int k = 0; k < od; k += kPushChunk, ++pos) {
+            if (pos < a.frontier_cap) a.frontier[pos] = make_int4(u, bits, k, 0);
+            else ctl->error = 2;
+          }
         }
       }
     }
