@@ -118,16 +118,34 @@ REFERENCE_MOUNT = "/root/reference"
 
 def build_oracle() -> None:
     """Compiles the oracle's CPU restatement; and the reference's own apps
-    when the reference tree is present on this machine."""
-    r = subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "oracle"], capture_output=True, text=True)
+    when the reference tree is present on this machine.  Where it is not but
+    the working tree carries the recipe's patched copies of the reference
+    sources (oracle/_ref/, never committed), the reference's PageRank app is
+    compiled from them for this host, as the CPU baseline; a host that cannot
+    compile it keeps the oracle's restatement as the baseline."""
+    oracle = ROOT / "oracle"
+    r = subprocess.run(["make", "-s", "-C", str(oracle), "oracle"], capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stdout}\n{r.stderr}")
     ref_root = os.environ.get("GX_REFERENCE_ROOT", REFERENCE_MOUNT)
     if Path(ref_root, "GraphMP", "system", "Comp.h").exists():
-        r = subprocess.run(["make", "-s", "-C", str(ROOT / "oracle"), "ref", f"REF={ref_root}"],
+        r = subprocess.run(["make", "-s", "-C", str(oracle), "ref", f"REF={ref_root}"],
                            capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"reference build failed:\n{r.stdout}\n{r.stderr}")
+    elif (oracle / "_ref" / "src_cached" / ".stamp").exists() and not _runs(oracle / "_ref" / "ref_pagerank_cached"):
+        subprocess.run(["make", "-s", "-C", str(oracle), "ref-from-copies"], capture_output=True, text=True)
+
+
+def _runs(binary: Path) -> bool:
+    """The binary exists and starts on this host (it prints its usage)."""
+    if not binary.exists():
+        return False
+    try:
+        r = subprocess.run([str(binary)], capture_output=True, text=True, timeout=30)
+    except OSError:
+        return False
+    return "usage" in r.stderr
 
 
 def build(force: bool = False) -> None:
