@@ -1704,10 +1704,7 @@ gx_status gx_get_values(gx_engine* e, void* host_out) {
     GX_TRY(values_to_caller(e, src, e->s_comp));
     src = e->d_stage;
   }
-  // Into the caller's buffer, written in place by the device where it reaches
-  // pageable memory (the host link's rate rather than a staged copy's).
-  GX_TRY(download_async(e, host_out, src, sizeof(uint32_t) * e->V, e->s_comp));
-  GX_CUDA(cudaStreamSynchronize(e->s_comp));
+  GX_CUDA(cudaMemcpy(host_out, src, sizeof(uint32_t) * e->V, cudaMemcpyDeviceToHost));
   return GX_OK;
 }
 
