@@ -312,12 +312,13 @@ int bits_for(int64_t n) {  // bits of the largest value below n
 __global__ void store_i64_kernel(int64_t* p, int64_t x) { *p = x; }
 
 // A relabelling load up to the move of the source ids: the caller's offsets
-// go to the device, which sorts the vertices into the new order, derives the
-// new offsets and out-degrees, and copies them and the permutation back for
-// the host's own planning (e->off, e->outdeg, h_perm: waited for here); the
-// source ids, uploaded meanwhile, are then renamed into place in one pass
-// (still running on the copy stream when this returns; flag bits as
-// validate_csc_kernel's).  Also counts the dangling vertices.
+// go to the device, which sorts the vertices into the new order and derives
+// the new offsets and out-degrees; the new offsets come back to the host for
+// its own planning (e->off, waited for here) while the source ids go up; the
+// ids are then renamed into place in one pass, and the out-degrees and the
+// permutation come back (e->outdeg, h_perm) — both still running on the copy
+// stream when this returns (flag bits as validate_csc_kernel's).  Also
+// counts the dangling vertices.
 // Device-side phases of a load, for the verbose log: events recorded on a
 // stream, their times printed relative to the first once the stream is done.
 struct StreamMarks {
@@ -420,18 +421,22 @@ gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, 
   host_resize_placed(e->off, static_cast<size_t>(V) + 1);
   host_resize_placed(e->outdeg, static_cast<size_t>(V));
   host_resize_placed(e->h_perm, static_cast<size_t>(V));
+  // The new offsets first (the host plans the work units from them while
+  // the ids go up); the out-degrees and the permutation, which the host
+  // needs only once the load is done, after the renaming.
   GX_TRY(download_async(e, e->off.data(), e->d_off, sizeof(int64_t) * (static_cast<size_t>(V) + 1), s));
-  GX_TRY(download_async(e, e->outdeg.data(), e->d_outdeg, sizeof(int32_t) * static_cast<size_t>(V), s));
-  GX_TRY(download_async(e, e->h_perm.data(), e->d_perm, sizeof(int32_t) * static_cast<size_t>(V), s));
   cudaEvent_t ev = nullptr;
   GX_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   std::unique_ptr<CUevent_st, cudaError_t (*)(cudaEvent_t)> evg(ev, cudaEventDestroy);
   GX_CUDA(cudaEventRecord(ev, s));
-  marks.mark("host copies", s);
+  marks.mark("host offsets", s);
   GX_CUDA(cudaStreamWaitEvent(s, ev_col, 0));
   marks.mark("ids ready", s);
   GX_TRY(relabel_scatter(e, sc.col_old, e->d_col, true, sc.longs, sc.n_longs, sc.flag, s));
   marks.mark("ids renamed", s);
+  GX_TRY(download_async(e, e->outdeg.data(), e->d_outdeg, sizeof(int32_t) * static_cast<size_t>(V), s));
+  GX_TRY(download_async(e, e->h_perm.data(), e->d_perm, sizeof(int32_t) * static_cast<size_t>(V), s));
+  marks.mark("host copies", s);
   GX_CUDA(cudaEventSynchronize(ev));
   return GX_OK;
 }
