@@ -374,10 +374,9 @@ gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, 
   GX_CUDA(cudaMemsetAsync(e->d_col + E, 0, 8 * sizeof(int32_t), s));
   // The offsets go up first and the device works out the order; then the
   // caller's source ids go up on the compute stream (idle during a load)
-  // while the new offsets, out-degrees and permutation come back to the
-  // host.  (Reading the ids in place list by list would take small,
-  // latency-bound host reads; an upload beside the sort slows the sort
-  // several times over.)
+  // while the new offsets come back to the host.  (Renaming the ids read in
+  // place from host memory took as long as this upload plus the renaming;
+  // an upload beside the sort slows the sort several times over.)
   cudaEvent_t ev_order = nullptr, ev_col = nullptr;
   GX_CUDA(cudaEventCreateWithFlags(&ev_order, cudaEventDisableTiming));
   std::unique_ptr<CUevent_st, cudaError_t (*)(cudaEvent_t)> ev_order_g(ev_order, cudaEventDestroy);
