@@ -63,6 +63,11 @@ def test_traffic_read_from_committed_profiles():
         t = bench.ncu_traffic(f"rmat{scale}")
         assert t is not None and t > 1e6, p.name
     assert bench.ncu_traffic("rmat99") is None
+    # The headline's layout reads its own capture: the relabelled pull
+    # kernel at the headline's scale moves less DRAM than the plain one.
+    relabelled, plain = bench.ncu_traffic("rmat26", "relabel"), bench.ncu_traffic("rmat26", "plain")
+    assert relabelled is not None and plain is not None and relabelled < plain
+    assert bench.layout_cfg("relabel") == {"relabel": 1} and bench.layout_cfg("plain") == {}
 
 
 def test_profile_summaries_name_their_commands():
