@@ -546,7 +546,7 @@ def run_cc_tc(args):
     t0 = time.time()
     g = gx.rmat_graph(args.scale, args.edge_factor, seed=SEED, P=SHARDS, symmetric=True, gpu=True)
     build_s = time.time() - t0
-    with gx.Engine() as e:
+    with gx.Engine(**layout_cfg(args.layout)) as e:
         e.load(g)
         for _ in range(args.warmup):
             e.run(gx.APP_CC, 10000)
@@ -567,7 +567,7 @@ def run_cc_tc(args):
           cpu_baseline={"value": g.E * len(ch) / cpu_s / 1e9, "unit": "GTEPS (entries x supersteps / s)",
                         "cores": os.cpu_count(), "kind": "port", "sample": "full CC run, same graph"},
           triangles=tri, tc_ms=min(st["ms_total"], st2["ms_total"]), tc_repeatable=tri == tri2,
-          tc_work_edges=st["edges_scanned"])
+          tc_work_edges=st["edges_scanned"], layout=args.layout)
 
 
 def pinned_h2d_gbs(nbytes=2 << 30, repeats=7):
