@@ -676,7 +676,7 @@ def run_ppr(args):
     g, build_s = build_graph(args, device=0)
     rng = np.random.default_rng(SEED)
     src = rng.integers(0, g.V, size=64).astype(np.int32)
-    with gx.Engine() as e:
+    with gx.Engine(**layout_cfg(args.layout)) as e:
         e.load(g)
         e.ppr(src, 2, fetch=False)
         runs = [e.ppr(src, args.iters, fetch=False)[1] for _ in range(args.steps)]
@@ -697,7 +697,7 @@ def run_ppr(args):
                     "algorithmic_bytes_per_step": alg},
           separate={"ms": ms_sep, "gteps": 64 * g.E * args.iters / (ms_sep / 1000) / 1e9,
                     "note": "64 calls of one source each (rows of 8 columns), one persistent launch per call"},
-          speedup_vs_separate=ms_sep / ms)
+          speedup_vs_separate=ms_sep / ms, layout=args.layout)
 
 
 def run_warm(args):
