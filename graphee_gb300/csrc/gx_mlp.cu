@@ -17,8 +17,10 @@
 // output approximates r where the L1 error lives.
 // Weights: FP32 master copy updated by Adam; every forward pass (training
 // and inference) uses the weights rounded to BF16, with FP32 accumulation.
-// Inference runs on the tensor cores (mma.sync m16n8k16 in f16, in which the
-// BF16-rounded weights are exact; each layer's accumulators re-packed in
+// Inference runs on the tensor cores (mma.sync m16n8k16 in f16, in which a
+// BF16-rounded weight is exact when its magnitude lies in [2^-17, 65504];
+// smaller ones land on f16's subnormal grid, an error below 2^-25, and larger
+// ones are clamped to 65504; each layer's accumulators re-packed in
 // registers as the next layer's A fragments, GELUs on packed f16 pairs,
 // layer 3 as an MMA against the w3 column); training runs
 // hand-written FP32 forward/backward kernels whose per-CTA weight gradients
@@ -251,6 +253,13 @@ __global__ void __launch_bounds__(256) mlp_heavy_features_kernel(const int64_t* 
   }
 }
 
+// A BF16-rounded weight as an f16 operand: exact for magnitudes in
+// [2^-17, 65504] (BF16's 8 significant bits fit f16's subnormal grid down to
+// 2^-17), rounded below that, clamped above it.
+__device__ __forceinline__ __half half_weight(float w) {
+  return __float2half_rn(fminf(fmaxf(bf16r(w), -65504.f), 65504.f));
+}
+
 __device__ __forceinline__ uint32_t pack_h2(float lo, float hi) {
   const __half2 h = __floats2half2_rn(lo, hi);
   return *reinterpret_cast<const uint32_t*>(&h);
@@ -280,10 +289,10 @@ __device__ __forceinline__ uint32_t gelu_h2(uint32_t xr) {
 }
 
 // Inference: 16 vertices per warp step on the tensor cores, all three layers
-// as f16 mma.sync m16n8k16 with FP32 accumulation.  The BF16-rounded weights
-// are exact in f16.  Each layer's accumulators plus bias are packed to f16x2
-// in registers, where they already sit as the next layer's A fragments; the
-// GELUs run on the packed pairs.  Layer 3 is an MMA against w3 as column 0
+// as f16 mma.sync m16n8k16 with FP32 accumulation, on the BF16-rounded
+// weights converted by half_weight.  Each layer's accumulators plus bias are
+// packed to f16x2 in registers, where they already sit as the next layer's A
+// fragments; the GELUs run on the packed pairs.  Layer 3 is an MMA against w3 as column 0
 // of an otherwise zero B, so lanes with t == 0 receive z of rows g and g+8.
 // Writes s_v = softplus(z_v) and each CTA's partial sums of s and of s over
 // dangling vertices.
@@ -297,16 +306,16 @@ __global__ void __launch_bounds__(128) mlp_infer_kernel(const float* feat, const
   __shared__ double s_red[2][4];
   for (int i = threadIdx.x; i < kH * 24; i += blockDim.x) {
     const int n = i / 24, k = i % 24;
-    sW1[n][k] = __float2half_rn(k < kF ? bf16r(params[kOffW1 + n * kF + k]) : 0.f);
+    sW1[n][k] = half_weight(k < kF ? params[kOffW1 + n * kF + k] : 0.f);
   }
   for (int i = threadIdx.x; i < kH * 72; i += blockDim.x) {
     const int n = i / 72, k = i % 72;
-    sW2[n][k] = __float2half_rn(k < kH ? bf16r(params[kOffW2 + n * kH + k]) : 0.f);
+    sW2[n][k] = half_weight(k < kH ? params[kOffW2 + n * kH + k] : 0.f);
   }
   for (int i = threadIdx.x; i < kH; i += blockDim.x) {
     sb1[i] = params[kOffB1 + i];
     sb2[i] = params[kOffB2 + i];
-    sw3[i] = __float2half_rn(bf16r(params[kOffW3 + i]));
+    sw3[i] = half_weight(params[kOffW3 + i]);
   }
   if (threadIdx.x == 0) sb3 = params[kOffB3];
   if (threadIdx.x < kF) {
