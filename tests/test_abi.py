@@ -42,6 +42,34 @@ def test_config_defaults():
     assert p.source == 1 and p.damping == pytest.approx(0.85)
 
 
+def test_python_structs_match_the_header():
+    """The ctypes mirrors of the ABI's structs have the C structs' size and
+    field offsets (a field added on one side only would shift every later
+    one)."""
+    import subprocess
+    import tempfile
+    structs = {"gx_config": gx.Config, "gx_run_params": gx.RunParams, "gx_run_stats": gx.RunStats,
+               "gx_iter_stats": gx.IterStats, "gx_batch_tuning": gx.BatchTuning, "gx_warm_stats": gx.WarmStats}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", "#include \"gx.h\"", "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for f, _ in py._fields_:
+            lines.append(f'  printf("{cname} {f} %zu\\n", offsetof({cname}, {f}));')
+    lines += ["  return 0;", "}"]
+    with tempfile.TemporaryDirectory() as d:
+        src, exe = Path(d) / "layout.c", Path(d) / "layout"
+        src.write_text("\n".join(lines) + "\n")
+        r = subprocess.run(["gcc", "-I", str(ROOT / "include"), str(src), "-o", str(exe)], capture_output=True,
+                           text=True)
+        assert r.returncode == 0, r.stderr
+        out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {tuple(x.split()[:2]): int(x.split()[2]) for x in out if x}
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == C.sizeof(py), cname
+        for f, _ in py._fields_:
+            assert got[(cname, f)] == getattr(py, f).offset, (cname, f)
+
+
 def test_null_arguments_are_errors():
     L = gx.lib()
     assert L.gx_create(None, None) == gx.GX_ERR_INVALID
