@@ -30,6 +30,60 @@ def rmat16():
     return gx.rmat_graph(16, 16, seed=41, P=32, weight_seed=7)
 
 
+def golden_graph(c):
+    return gx.Graph(int(c["V"]), c["off"], c["col"], c["outdeg"], int(c["P"]), c["bounds"])
+
+
+def test_reference_golden_vectors(golden_cases):
+    """The reference's own outputs (its compiled apps on the fixtures: R-MAT,
+    a path, a 3000-in-edge hub, components with self-loops and isolated
+    vertices, empty shards), reproduced by a relabelled engine: PageRank in
+    exact-order mode, SSSP from vertices 1 and 0 (push on and off) and CC,
+    values and per-step counts bit for bit."""
+    for name, c in golden_cases.items():
+        g = golden_graph(c)
+        with gx.Engine(exact_order=1, **RL) as e:
+            e.load(g)
+            st = e.run(gx.APP_PAGERANK_REF, 20)
+            assert np.array_equal(e.values().view(np.uint32), c["pr"].view(np.uint32)), name
+            assert np.array_equal(counts(e, st["iterations"]), c["pr_changed"]), name
+        for push in (1, 0):
+            with gx.Engine(push_sparse=push, **RL) as e:
+                e.load(g)
+                for source in (1, 0):
+                    st = e.run(gx.APP_SSSP, 200, source=source)
+                    assert np.array_equal(e.values(), c[f"sssp{source}"]), (name, push, source)
+                    assert np.array_equal(counts(e, st["iterations"]), c[f"sssp{source}_changed"]), (name, push)
+                st = e.run(gx.APP_CC, 200)
+                assert np.array_equal(e.values(), c["cc"]), (name, push)
+                assert np.array_equal(counts(e, st["iterations"]), c["cc_changed"]), (name, push)
+
+
+@pytest.mark.parametrize("P", [1, 1024])
+def test_one_shard_and_tiny_shards(P):
+    """One shard (the whole graph renumbered as one) and shards of four
+    vertices: PageRank exact-order, weighted SSSP and CC bit-exact."""
+    g = gx.rmat_graph(12, 16, seed=5, P=P, weight_seed=3)
+    ref, ch, _ = O.run(O.PAGERANK_REF, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 20)
+    dist, dch, _ = O.run(O.SSSP, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 1000, weights=g.weights, source=0)
+    with gx.Engine(exact_order=1, **RL) as e:
+        e.load(g)
+        st = e.run(gx.APP_PAGERANK_REF, 20)
+        assert np.array_equal(e.values().view(np.uint32), ref.view(np.uint32))
+        assert np.array_equal(counts(e, st["iterations"]), ch)
+        e.set_weights(g.weights)
+        st = e.run(gx.APP_SSSP, 1000, source=0, weighted=True)
+        assert np.array_equal(e.values(), dist)
+        assert np.array_equal(counts(e, st["iterations"]), dch)
+    gs = gx.rmat_graph(12, 8, seed=6, P=P, symmetric=True)
+    lab, lch, _ = O.run(O.CC, gs.V, gs.P, gs.bounds, gs.off, gs.col, gs.outdeg, 1000)
+    with gx.Engine(**RL) as e:
+        e.load(gs)
+        st = e.run(gx.APP_CC, 1000)
+        assert np.array_equal(e.values(), lab)
+        assert np.array_equal(counts(e, st["iterations"]), lch)
+
+
 def test_pagerank_exact_order_bitexact(rmat16):
     g = rmat16
     ref, ch, _ = O.run(O.PAGERANK_REF, g.V, g.P, g.bounds, g.off, g.col, g.outdeg, 20)
