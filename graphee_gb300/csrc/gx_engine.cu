@@ -315,10 +315,10 @@ __global__ void store_i64_kernel(int64_t* p, int64_t x) { *p = x; }
 // go to the device, which sorts the vertices into the new order and derives
 // the new offsets and out-degrees; the new offsets come back to the host for
 // its own planning (e->off, waited for here) while the source ids go up; the
-// ids are then renamed into place in one pass while the out-degrees and the
-// permutation come back (e->outdeg, h_perm) — both still running when this
-// returns, and both ahead of the copy stream's end (flag bits as
-// validate_csc_kernel's).  Also counts the dangling vertices.
+// ids are then renamed into place in one pass, and the out-degrees and the
+// permutation come back (e->outdeg, h_perm) — both still running on the copy
+// stream when this returns (flag bits as validate_csc_kernel's).  Also
+// counts the dangling vertices.
 // Device-side phases of a load, for the verbose log: events recorded on a
 // stream, their times printed relative to the first once the stream is done.
 struct StreamMarks {
@@ -433,16 +433,9 @@ gx_status relabel_load(gx_engine* e, const int32_t* bounds, const int64_t* off, 
   marks.mark("ids ready", s);
   GX_TRY(relabel_scatter(e, sc.col_old, e->d_col, true, sc.longs, sc.n_longs, sc.flag, s));
   marks.mark("ids renamed", s);
-  // Beside the renaming, on the compute stream behind the ids' upload; the
-  // copy stream (whose end the load waits for) then waits for them too.
-  cudaEvent_t ev_down = nullptr;
-  GX_CUDA(cudaEventCreateWithFlags(&ev_down, cudaEventDisableTiming));
-  std::unique_ptr<CUevent_st, cudaError_t (*)(cudaEvent_t)> ev_down_g(ev_down, cudaEventDestroy);
-  GX_TRY(download_async(e, e->outdeg.data(), e->d_outdeg, sizeof(int32_t) * static_cast<size_t>(V), e->s_comp));
-  GX_TRY(download_async(e, e->h_perm.data(), e->d_perm, sizeof(int32_t) * static_cast<size_t>(V), e->s_comp));
-  GX_CUDA(cudaEventRecord(ev_down, e->s_comp));
-  marks.mark("host copies", e->s_comp);
-  GX_CUDA(cudaStreamWaitEvent(s, ev_down, 0));
+  GX_TRY(download_async(e, e->outdeg.data(), e->d_outdeg, sizeof(int32_t) * static_cast<size_t>(V), s));
+  GX_TRY(download_async(e, e->h_perm.data(), e->d_perm, sizeof(int32_t) * static_cast<size_t>(V), s));
+  marks.mark("host copies", s);
   GX_CUDA(cudaEventSynchronize(ev));
   return GX_OK;
 }
